@@ -1,0 +1,422 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 flock step: bird-updates/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Headline (`value`): the plain single-flock step at 1,000,000 birds (seed 1,
+the reference's benchmark scatter), K timed steps after W warm-up steps, each
+timed step launched alone (one CUDA graph) after a 256 MB write that flushes
+the 129 MB L2, device time from CUDA events on the library's stream.
+
+Also on the same line:
+  e2e        the same workload through the C ABI from pinned host buffers
+             (upload, K steps, download inside the timed region);
+  roofline   step bytes (B_alg per bird-update) / step time vs measured HBM peak;
+  batched    256 flocks, sizes log-uniform in [1e3, 2e5] (seed 3), 10-step
+             graph chunks, against the same flocks run one at a time;
+  served     a Poisson stream of simulate(flock, steps) requests (seed 5)
+             through the continuous-batching pool: p50/p99 latency and
+             aggregate bird-updates/s, against the same requests served one
+             at a time through the plain step;
+  cpu_baseline  the brute-force CPU oracle on a bounded sample of the workload.
+
+`--impl reference` times the reference's own CPU step (the C restatement of
+its flock-ref oracle; the Rust original cannot be built on this image) on all
+host cores, on a bounded sample of the same workload per step.
+
+Multi-GPU (torchrun, one rank per GPU): independent replicas of the plain
+workload (a single flock does not shard; flocks would be partitioned across
+GPUs with no exchange), barrier + max over ranks, value = all ranks' updates.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bird-updates/s/GPU plain vs batched-served; p50/p99 request latency"
+WORDS = 15
+FLUSH_BYTES = 256 << 20
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic_step_1m.txt")
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def peak_hbm() -> tuple[float, str]:
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def step_traffic_bytes() -> float | None:
+    """DRAM bytes (read + write) of one 1M-bird step from the committed ncu summary."""
+    try:
+        for line in open(TRAFFIC):
+            if line.startswith("step_dram_bytes"):
+                return float(line.split("=")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict | None:
+        if not self.proc or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4) if r[k].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    """torch.distributed only under torchrun (N > 1)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None, 0, 1, 0
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return dist, rank, world, local
+
+
+def aggregate(dist, local_ms: float, local_units: float) -> tuple[float, float]:
+    """Max time over ranks, sum of work over ranks (replicas)."""
+    if dist is None:
+        return local_ms, local_units
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_ms], dtype=torch.float64, device=dev)
+    u = torch.tensor([local_units], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def log_uniform_sizes(rng, count, lo, hi):
+    return np.rint(np.exp(rng.uniform(math.log(lo), math.log(hi), size=count))).astype(np.int64)
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (brute-force oracle) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(words: np.ndarray, budget_s: float, seed: int = 0) -> dict:
+    """Decide for a random sample of deciding birds (brute force over all N) plus
+    integrate of all N, extrapolated to one full step; all host threads."""
+    from oracle import pyoracle as o
+
+    n = len(words)
+    due = np.nonzero(np.float32(0.005) >= words[:, 12])[0]
+    threads = o.max_threads()
+    rng = np.random.default_rng(seed)
+    probe = rng.choice(due, size=min(len(due), max(threads, 16)), replace=False)
+    t0 = time.perf_counter()
+    o.decide_sample(words, probe)
+    per_bird = (time.perf_counter() - t0) / len(probe)
+    m = int(min(len(due), max(len(probe), budget_s / max(per_bird, 1e-9))))
+    sample = rng.choice(due, size=m, replace=False)
+    t0 = time.perf_counter()
+    o.decide_sample(words, sample)
+    t_dec = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.integrate_all(words)
+    t_int = time.perf_counter() - t0
+    step_s = t_dec * len(due) / m + t_int
+    return {"value": n / step_s, "unit": "bird-updates/s", "cores": threads, "kind": "port",
+            "sample": f"brute-force decide of {m} of the {len(due)} deciding birds (each against all {n}) "
+                      f"+ integrate of all {n}; extrapolated to one step ({step_s:.3f} s)",
+            "sample_wall_s": round(t_dec + t_int, 3)}
+
+
+def run_reference(args, dist, rank):
+    if rank != 0:
+        return
+    from oracle import pyoracle as o
+
+    words = o.scatter(args.birds, args.seed)
+    per_step = max(0.05, 90.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_sample(words, 0.02)
+    vals, walls = [], []
+    for s in range(args.steps):
+        r = cpu_sample(words, per_step, seed=s)
+        vals.append(r["value"])
+        walls.append(r["sample_wall_s"])
+    step_s = statistics.mean(args.birds / v for v in vals)
+    value = args.birds / step_s
+    out = {"metric": METRIC, "impl": "reference", "value": value, "unit": "bird-updates/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (flock-ref gen scatter)",
+           "config": {"workload": f"plain single-flock step, {args.birds:,} birds, seed {args.seed}",
+                      "birds": args.birds, "seed": args.seed},
+           "cpu_baseline": {"value": value, "unit": "bird-updates/s", "cores": r["cores"], "kind": "port",
+                            "sample": f"per step: {r['sample']}; mean over {args.steps} steps"},
+           "e2e": {"value": value, "unit": "bird-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def bench_plain(m, args, dist, local):
+    n, K, W = args.birds, args.steps, max(3, args.warmup)
+    words = m.generate(n, args.seed)
+    f = m.Flock(words, 0.0, device=local)
+    f.step(W)
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        ms = f.time_steps(K, FLUSH_BYTES)
+    barrier(dist)
+    total_ms = float(ms.sum())
+    due0, cand0, pairs0 = f.counters()
+    # per-pass shares from an eager run with events between passes (same state continues)
+    passes = f.step_timed(10, 0)
+    due1, cand1, pairs1 = f.counters()
+    f.close()
+    return dict(ms=ms, total_ms=total_ms, clocks=clk.summary(), passes=passes,
+                due_frac=(due1 - due0) / (10 * n), cand_per_due=(cand1 - cand0) / max(1, due1 - due0),
+                pairs_per_due=(pairs1 - pairs0) / max(1, due1 - due0), due_total=due0)
+
+
+def bench_e2e(m, args, local):
+    """Through the C ABI with host buffers: upload, K steps, download."""
+    n, K = args.birds, args.steps
+    words = m.generate(n, args.seed)
+    out = np.empty_like(words)
+    with m.pinned(words, out):
+        # one untimed pass first so lazy CUDA initialisation is not timed
+        g = m.Flock(words[:1024].copy(), 0.0, device=local)
+        g.step(1)
+        g.close()
+        t0 = time.perf_counter()
+        f = m.Flock(words, 0.0, device=local)
+        f.step(K)
+        f.read(out)
+        t1 = time.perf_counter()
+        f.close()
+    s = t1 - t0
+    return {"value": n * K / s, "unit": "bird-updates/s", "h2d_bytes_per_step": n * WORDS * 4 / K,
+            "d2h_bytes_per_step": n * WORDS * 4 / K,
+            "how": f"flk_open_host (H2D of {n * 60 / 1e6:.0f} MB, pinned) + flk_step({K}) + flk_read_host "
+                   f"(D2H) through the C ABI, host wall clock {s * 1e3:.1f} ms"}
+
+
+def bench_batched(m, args, local):
+    rng = np.random.default_rng(3)
+    sizes = log_uniform_sizes(rng, 256, 1_000, 200_000)
+    K = args.batched_steps
+    flocks = [m.generate(int(nf), 3 + k) for k, nf in enumerate(sizes)]
+    total = int(sizes.sum())
+    b = m.Batch(device=local)
+    for w in flocks:
+        b.add(w)
+    b.step(10)  # warm-up (graph capture)
+    ms_batched = b.time_steps(K)
+    b.close()
+    # the same flocks one at a time through the plain step (same graphs, one flock each)
+    ms_plain = 0.0
+    for w in flocks:
+        p = m.Batch(device=local)
+        p.add(w)
+        p.step(10)
+        ms_plain += p.time_steps(K)
+        p.close()
+    v_b = total * K / (ms_batched / 1e3)
+    v_p = total * K / (ms_plain / 1e3)
+    return {"value": v_b, "unit": "bird-updates/s", "flocks": 256, "birds": total, "steps": K,
+            "ms_per_step": ms_batched / K, "plain_one_at_a_time": v_p, "speedup_vs_plain": v_b / v_p,
+            "config": "256 flocks, n log-uniform [1e3, 2e5] (seed 3), flock k seed 3+k, 10-step CUDA graphs"}
+
+
+def bench_served(m, args, local):
+    rng = np.random.default_rng(5)
+    R = args.requests
+    sizes = log_uniform_sizes(rng, R, 2_000, 1_000_000)
+    steps = rng.integers(10, 501, size=R)
+    gaps = rng.exponential(1.0 / args.rate, size=R)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    states = [m.generate(int(nf), 5 + k) for k, nf in enumerate(sizes)]
+    outs = [np.empty_like(w) for w in states]
+    demand = float(np.sum(sizes * steps))
+    budget = 150 << 30
+    lat = [0.0] * R
+    with m.pinned(*states, *outs):
+        with m.Pool(budget, chunk_steps=args.chunk, device=local) as pool:
+            # warm the pool (graph capture, CUDA init) with a tiny request
+            pool.wait(pool.submit(m.generate(1000, 99), 12))
+            tickets = [None] * R
+            t0 = time.perf_counter()
+
+            def feeder():
+                for k in range(R):
+                    dt = t0 + arrivals[k] - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets[k] = pool.submit(states[k], int(steps[k]), out=outs[k])
+
+            th = threading.Thread(target=feeder)
+            th.start()
+            th.join()
+            for k in range(R):
+                _, _, lat[k] = pool.wait(tickets[k])
+            t_end = time.perf_counter()
+        span = t_end - t0
+    # the same requests one at a time through the plain step, FCFS on the same arrivals
+    service = []
+    for k in range(R):
+        s0 = time.perf_counter()
+        f = m.Flock(states[k], 0.0, device=local)
+        f.step(int(steps[k]))
+        f.read(outs[k])
+        f.close()
+        service.append(time.perf_counter() - s0)
+    finish, lat_seq = 0.0, []
+    for k in range(R):
+        start = max(arrivals[k], finish)
+        finish = start + service[k]
+        lat_seq.append((finish - arrivals[k]) * 1e3)
+    span_seq = finish - arrivals[0]
+    p = lambda xs, q: float(np.percentile(np.asarray(xs), q))
+    return {"value": demand / span, "unit": "bird-updates/s", "requests": R, "rate_per_s": args.rate,
+            "p50_ms": p(lat, 50), "p99_ms": p(lat, 99),
+            "sequential_plain": {"value": demand / span_seq, "p50_ms": p(lat_seq, 50), "p99_ms": p(lat_seq, 99)},
+            "speedup_vs_plain": (demand / span) / (demand / span_seq),
+            "config": f"Poisson arrivals {args.rate}/s (seed 5), n log-uniform [2e3, 1e6], steps U[10, 500], "
+                      f"150 GB admission budget, {args.chunk}-step fold-in chunks"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--birds", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched / served / CPU measurements")
+    ap.add_argument("--batched-steps", type=int, default=30)
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--rate", type=float, default=40.0)
+    ap.add_argument("--chunk", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    args = ap.parse_args()
+
+    dist, rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, dist, rank)
+        return
+
+    import murmuration_kernels_gb300 as m
+
+    r = bench_plain(m, args, dist, local)
+    n, K = args.birds, args.steps
+    ms_max, units = aggregate(dist, r["total_ms"], float(n * K))
+    value = units / (ms_max / 1e3)
+    ms_per_step = ms_max / K
+    f = r["due_frac"]
+    b_alg = 60 + 32 + 28 * f + 16
+    peak, peak_kind = peak_hbm()
+    achieved = b_alg * n / (ms_per_step / 1e3) / 1e9
+    traffic = step_traffic_bytes()
+    out = {
+        "metric": METRIC, "value": value, "unit": "bird-updates/s", "n_gpus": world, "steps": K,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (flock-ref gen scatter: SplitMix64, density 0.5)",
+        "config": {"workload": f"plain single-flock step, {n:,} birds, seed {args.seed}", "birds": n,
+                   "seed": args.seed, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch"},
+        "roofline": {"bound": "hbm", "kernel": "whole step (6 passes, one graph launch)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,
+                     "traffic": traffic},
+        "passes_ms": {k: round(v, 5) for k, v in r["passes"].items() if k.endswith("_ms")},
+        "decide": {"candidates_per_deciding_bird": r["cand_per_due"], "pairs_in_2R_per_deciding_bird":
+                   r["pairs_per_due"]},
+        "gpu_launches": m.kernels_per_step() * K,
+        "clocks": r["clocks"],
+        "step_ms_p50": float(np.median(r["ms"])), "step_ms_min": float(r["ms"].min()),
+    }
+    if rank == 0:
+        out["e2e"] = bench_e2e(m, args, local)
+        if not args.no_extra:
+            out["batched"] = bench_batched(m, args, local)
+            out["served"] = bench_served(m, args, local)
+            out["cpu_baseline"] = cpu_sample(m.generate(n, args.seed), args.cpu_budget)
+        print(json.dumps(out), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

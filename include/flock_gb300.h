@@ -1,0 +1,165 @@
+/*
+ * flock_gb300.h -- C ABI of the GB300-native starling-flock step.
+ *
+ * The reference (ImanolGo/murmuration-kernels) exposes its GPU step only as an
+ * executable contract: `flock_cuda --in F [--steps K] [--warmup W] [--out F]`
+ * reading and writing the FLK1 state file (cuda/flock.cu:374-523,
+ * crates/flock-ref/src/state.rs:104-171). Each entry point below replaces one
+ * piece of that program, so a host in any language (the reference's Rust
+ * crates through a thin FFI, Python through ctypes, the bundled CLI) can drive
+ * the step in-process. Plain pointers and sizes only; no CUDA or torch types.
+ *
+ * State words: a flock of n birds is n*15 little-endian 4-byte words in the
+ * .flk record order (state.rs:1-7): pos xyz, vel xyz, roll, spin, radius,
+ * steering xyz, next_decision, neighbour count (u32 bits), centrality.
+ *
+ * Conventions: every call returns FLK_OK (0) or a negative FLK_ERR_* code and
+ * never exits the process; flk_last_error() gives the calling thread's last
+ * message. The library owns device memory; the caller owns host buffers and
+ * states are copied in and out. A flock handle is used by one thread at a
+ * time; a pool is internally synchronised. Device-side failures (a scan wait
+ * that gave up) surface as FLK_ERR_DEVICE from the call that ran the step.
+ */
+#ifndef FLOCK_GB300_H
+#define FLOCK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLK_OK 0
+#define FLK_ERR_ARG -1      /* bad argument (null pointer, size) */
+#define FLK_ERR_IO -2       /* file open/read/write failed, truncated file */
+#define FLK_ERR_CUDA -3     /* a CUDA runtime call failed */
+#define FLK_ERR_ID -4       /* unknown flock id or ticket */
+#define FLK_ERR_CAPACITY -5 /* a batch exceeds the index space */
+#define FLK_ERR_DEVICE -6   /* the device error word was set during a step */
+#define FLK_ERR_FORMAT -7   /* not a FLK1 file with 15 words per bird */
+#define FLK_ERR_BUDGET -8   /* request can never fit the pool's memory budget */
+
+#define FLK_WORDS 15
+
+/* ---- plain single-flock step (the drop-in for flock_cuda) ---------------- */
+typedef struct flk_flock flk_flock;
+
+/* Mean GPU ms per pass over the timed steps, the reference's stdout table
+ * (cuda/flock.cu:474-492): hash+count, scan, scatter+sort, decide, integrate. */
+typedef struct {
+    double hash_ms, scan_ms, sort_ms, decide_ms, integrate_ms, total_ms;
+    int32_t timed_steps;
+} flk_pass_times;
+
+/* Uploads a flock from host words (replaces read_flk + the H2D copies,
+ * cuda/flock.cu:391,414-437). device < 0 uses the current device. */
+int flk_open_host(int32_t device, uint32_t n, float time, const float* words, flk_flock** out);
+/* Reads a .flk file and uploads it (cuda/flock.cu:340-354). */
+int flk_open_file(int32_t device, const char* path, flk_flock** out);
+/* Advances `steps` steps (the step loop, cuda/flock.cu:453-470); returns
+ * after the work is queued and checked (synchronises). */
+int flk_step(flk_flock* f, uint32_t steps);
+/* Same, launched pass by pass with CUDA events; fills the per-pass means of
+ * the last steps-warmup steps (cuda/flock.cu:447-492). */
+int flk_step_timed(flk_flock* f, uint32_t steps, uint32_t warmup, flk_pass_times* out);
+/* Copies the state back (replaces the D2H copies, cuda/flock.cu:494-519). */
+int flk_read_host(flk_flock* f, float* time, float* words);
+/* Writes the state as a .flk file (cuda/flock.cu:356-364). */
+int flk_write_file(flk_flock* f, const char* path);
+/* Bird count and canonical bucket count (cuda/flock.cu:368-372). */
+int flk_size(const flk_flock* f, uint32_t* n, uint32_t* buckets);
+/* Runs ONE step and returns the grid it built and the neighbour-set summary
+ * of every deciding bird, for bit-exact parity checks:
+ *   keys[n]          bucket of each bird (cuda/flock.cu:118-124 grid_histogram)
+ *   offsets[B+1]     exclusive scan of the bucket counts (grid_scan_*)
+ *   sorted[n]        birds in (bucket, bird index) order (grid_scatter, made stable)
+ *   sets[8n]         per bird: n_all, n_star, n_align, n_g and a wrapping sum of
+ *                    mix(j) over each of those sets (model.rs:67-115); zeros for
+ *                    birds that did not decide.
+ * Any output pointer may be NULL. */
+int flk_step_debug(flk_flock* f, uint32_t* keys, uint32_t* offsets, uint32_t* sorted, uint32_t* sets);
+/* Cumulative deciding birds, candidate tests and pairs within 2R. */
+int flk_counters(flk_flock* f, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
+/* Measurement helper (no counterpart in the reference, whose main() times
+ * passes inline, cuda/flock.cu:447-492): runs `steps` steps one graph launch
+ * at a time; before each step it overwrites a `flush_bytes` device buffer so
+ * the step starts with a cold L2, then brackets the step with CUDA events on
+ * the library's stream. ms_per_step[steps] receives each step's device time. */
+int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step);
+void flk_close(flk_flock* f);
+
+/* ---- batched: many independent flocks, one launch per pass --------------- */
+typedef struct flk_batch flk_batch;
+
+int flk_batch_create(int32_t device, flk_batch** out);
+/* Adds a flock; *id receives its handle within the batch. */
+int flk_batch_add(flk_batch* b, uint32_t n, float time, const float* words, int32_t* id);
+int flk_batch_remove(flk_batch* b, int32_t id);
+/* Advances every flock in the batch by `steps` steps (10-step CUDA graphs). */
+int flk_batch_step(flk_batch* b, uint32_t steps);
+/* Steps only the listed flocks, each by its own count (0 = idle). */
+int flk_batch_step_each(flk_batch* b, const int32_t* ids, const uint32_t* steps, uint32_t count);
+int flk_batch_read(flk_batch* b, int32_t id, float* time, float* words);
+/* One step of every flock; per-flock grid/sets outputs concatenated in id
+ * order of `ids` (same layouts as flk_step_debug, offsets per flock B_f+1). */
+int flk_batch_step_debug(flk_batch* b, const int32_t* ids, uint32_t count, uint32_t* keys, uint32_t* offsets,
+                         uint32_t* sorted, uint32_t* sets);
+/* Launch shape: CTAs per SM of the streaming passes and decide, decide CTA
+ * size, steps per captured graph. Zero keeps the current value. */
+int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t decide_threads, int32_t graph_chunk);
+int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
+/* Times `steps` graph-launched steps on the batch's stream with CUDA events. */
+int flk_batch_time_steps(flk_batch* b, uint32_t steps, double* ms);
+void flk_batch_destroy(flk_batch* b);
+
+/* ---- served: continuous batching of simulate(flock, steps) requests ------ */
+typedef struct flk_pool flk_pool;
+
+typedef struct {
+    uint64_t submitted, completed, rejected;
+    uint64_t bird_steps;     /* sum of n * steps over completed requests */
+    uint64_t resident_bytes; /* device bytes held by admitted flocks */
+    uint64_t chunks;         /* batched chunks run */
+    double busy_ms;          /* wall time the worker spent with work in flight */
+} flk_pool_stats;
+
+/* A worker thread owns the device; `budget_bytes` caps the device memory of
+ * admitted flocks; arrivals join the batch at chunk boundaries every
+ * `chunk_steps` steps. */
+int flk_pool_create(int32_t device, uint64_t budget_bytes, uint32_t chunk_steps, flk_pool** out);
+/* Queues simulate(flock, steps). `words` must stay valid until the request
+ * completes; the result (and its clock) are written to `out_words` /
+ * `out_time`, which may alias the input. */
+int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float* words, uint32_t steps, float* out_words,
+                    float* out_time, uint64_t* ticket);
+/* *state: 0 queued, 1 resident, 2 done, negative FLK_ERR_* on failure. */
+int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state);
+/* Blocks until done; *latency_ms = completion - submission (host clock). */
+int flk_pool_wait(flk_pool* p, uint64_t ticket, double* latency_ms);
+int flk_pool_stats_get(flk_pool* p, flk_pool_stats* out);
+void flk_pool_destroy(flk_pool* p);
+
+/* ---- helpers -------------------------------------------------------------- */
+const char* flk_last_error(void);
+/* Canonical bucket count: next power of two >= 2n clamped to [2^16, 2^22]. */
+uint32_t flk_buckets_for(uint32_t n);
+/* The benchmark scatter (state.rs:79-101): n birds, SplitMix64 seed. */
+int flk_generate(uint32_t n, uint64_t seed, float* words);
+/* Model constants in the order DT, DU, V0, MASS, CL_CD, G, L0, D0, TAU,
+ * TAU_ROLL, MAX_ROLL_RATE, MAX_BANK, V_MIN, V_MAX, N_C, R_MAX, RADIUS_LERP,
+ * R_H, SIGMA, W_SEP, W_ALIGN, W_COH, BLIND_COS, W_ROOST_V, H_ROOST_V, Z0,
+ * GRID_CELL, RADIUS_EXP (params.rs:5-65). Returns the count written. */
+int flk_params(float* out, int32_t cap);
+/* Device bytes a flock of n birds occupies when resident. */
+uint64_t flk_bytes_for(uint32_t n);
+/* Engine kernel launches per step (for launch accounting). */
+int flk_kernels_per_step(void);
+/* Page-locks / releases a caller's host buffer so state copies run at full
+ * link speed (cudaHostRegister / cudaHostUnregister). */
+int flk_pin(void* ptr, uint64_t bytes);
+int flk_unpin(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

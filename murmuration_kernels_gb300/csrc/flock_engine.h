@@ -1,0 +1,182 @@
+// Internal C++ interface of the GB300 flock engine: a resident arena of one
+// or more flocks and the per-step passes that advance all of them in one
+// launch per pass. The plain single-flock step, the batched step and the
+// serving pool are all this engine with one, many or a changing set of flocks,
+// so a flock's result does not depend on what else is resident.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace flk {
+
+// One flock in the device flock table (rebuilt whenever the resident set changes).
+struct FlockDesc {
+    uint32_t vbase;      // first virtual bird index (concatenation of table entries)
+    uint32_t n;          // birds
+    uint32_t sbase;      // first storage slot in the arena
+    uint32_t bbase;      // first global bucket
+    uint32_t buckets;    // power of two, buckets_for(n)
+    uint32_t remaining;  // steps still to run; 0 = idle this step
+    float time;          // world clock (f32, as the reference keeps it)
+    uint32_t pad;
+};
+
+// Step-control block in device memory: per-step counters (reset by the last
+// block of the integrate pass), the scan epoch and the device error word.
+struct StepCtl {
+    uint32_t occ_count;    // occupied buckets found this step
+    uint32_t due_count;    // deciding birds this step
+    uint32_t scan_ticket;  // dynamic tile ids of the scan
+    uint32_t epoch;        // scan status tag, advanced once per step
+    uint32_t done_blocks;  // integrate's last-block detector
+    uint32_t error;        // first device error (FLK_DEV_*), 0 = none
+    uint32_t err_info;
+    uint32_t pad;
+    unsigned long long due_total;   // cumulative deciding birds
+    unsigned long long cand_total;  // cumulative candidate tests in decide
+    unsigned long long pair_total;  // cumulative pairs inside 2R
+    unsigned long long pad2;
+};
+
+enum DeviceError : uint32_t {
+    DEV_OK = 0,
+    DEV_SCAN_TIMEOUT = 1,  // a scan look-back wait gave up
+    DEV_BAD_RANGE = 2,     // a bucket range or slot fell outside its array (skipped, not accessed)
+};
+
+// Per-pass timing of a step, mean ms over the timed steps (reference's table).
+struct PassTimes {
+    double ms[5];  // hash+count, scan, scatter+segment sort, decide, integrate
+    double total_ms;
+    int timed_steps;
+};
+
+// Sizes of the engine's launch shapes; chosen by the autotuner or defaults.
+struct LaunchShape {
+    int stream_blocks_per_sm = 8;   // bird-parallel passes: 256-thread CTAs per SM
+    int decide_threads = 256;       // threads per decide CTA
+    int decide_blocks_per_sm = 8;   // decide CTAs per SM
+    int segsort_blocks_per_sm = 8;  // segment-sort CTAs per SM (256 threads)
+    int graph_chunk = 10;           // steps per captured CUDA graph
+};
+
+struct GridDebug {  // host copies of one step's grid and neighbour-set summaries
+    std::vector<uint32_t> keys, offsets, sorted;  // per flock: n, buckets+1, n
+    std::vector<uint32_t> sets;                   // 8 words per bird (zeros for non-deciding birds)
+};
+
+class Engine {
+public:
+    explicit Engine(int device = -1);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    // Flocks. `words` is a host array of n*15 .flk words (any host memory).
+    int add_flock(uint32_t n, float time, const float* words);  // returns id >= 0
+    void remove_flock(int id);
+    void read_flock(int id, float* time, float* words);  // D2H + pack
+    float flock_time(int id);
+    uint32_t flock_size(int id) const;
+    bool has_flock(int id) const;
+    std::vector<int> flock_ids() const;
+
+    // Sets how many steps each listed flock still has to run (others: 0).
+    void set_remaining(const std::vector<int>& ids, const std::vector<uint32_t>& steps);
+    // Sets one flock's remaining steps, leaving the others as they are.
+    void set_flock_remaining(int id, uint32_t steps);
+    uint32_t flock_remaining(int id);
+    std::vector<uint32_t> remaining_of(const std::vector<int>& ids);  // one device read for all
+    // run(steps) bracketed by CUDA events on the engine stream; returns ms.
+    double time_run(uint32_t steps);
+    // `steps` single-step graph launches, each after overwriting `flush_bytes`
+    // of device memory (cold L2), each bracketed by events; ms per step.
+    void time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_step);
+    // Runs `steps` batched steps over the resident flocks (each flock stops
+    // when its remaining count reaches zero). Uses captured CUDA graphs.
+    void run(uint32_t steps);
+    // Eager steps with per-pass events (the reference's timing table).
+    void run_timed(uint32_t steps, uint32_t warmup, PassTimes* out);
+    // One eager step that also returns every flock's grid and set summaries.
+    void step_debug(std::vector<GridDebug>* out);
+    void sync();
+    uint32_t check_device_error();  // returns and clears the device error word
+
+    cudaStream_t stream() const { return stream_; }
+    int device() const { return device_; }
+    int num_sms() const { return num_sms_; }
+    LaunchShape& shape() { return shape_; }
+    void set_shape(const LaunchShape& s);
+    size_t device_bytes() const { return dev_bytes_; }
+    // Cumulative counters from the step-control block.
+    void counters(unsigned long long* due, unsigned long long* cand, unsigned long long* pairs);
+    // Bytes of device memory a flock of n birds would add (state + scratch).
+    static size_t bytes_for(uint32_t n);
+    // Launches of engine kernels per step (for the bench's launch count).
+    static int kernels_per_step() { return 6; }
+
+private:
+    struct Slot {
+        uint32_t n = 0, sbase = 0, buckets = 0, remaining = 0;
+        float time = 0.f;
+        bool live = false;
+    };
+    void ensure_arena(uint32_t need);
+    void rebuild_table();
+    void ensure_scratch();
+    void enqueue_step(bool sets, cudaEvent_t* ev = nullptr);
+    void free_graphs();
+    void ensure_graph();
+    void sync_times();
+
+    int device_ = 0, num_sms_ = 0;
+    cudaStream_t stream_ = nullptr;
+    LaunchShape shape_;
+    size_t dev_bytes_ = 0;
+
+    // arena (storage order)
+    uint32_t cap_ = 0, used_ = 0;
+    float4 *A_ = nullptr, *B_ = nullptr, *C_ = nullptr, *D_ = nullptr;
+    std::vector<Slot> slots_;
+    std::vector<std::pair<uint32_t, uint32_t>> free_ranges_;  // (sbase, n) holes
+
+    // flock table of flocks with remaining > 0, in slot order
+    bool table_dirty_ = true;
+    std::vector<FlockDesc> table_h_;
+    std::vector<int> table_ids_;
+    FlockDesc* table_d_ = nullptr;
+    uint32_t table_cap_ = 0;
+    uint32_t V_ = 0, Btot_ = 0;
+
+    // scratch (virtual / sorted order)
+    uint32_t scratch_V_ = 0, scratch_B_ = 0;
+    uint32_t *key_ = nullptr, *arrival_ = nullptr, *tmp_ = nullptr, *sorted_ = nullptr, *occ_ = nullptr;
+    uint2* due_ = nullptr;
+    float4 *spos_ = nullptr, *sfwd_ = nullptr;
+    uint32_t *counts_ = nullptr, *offsets_ = nullptr;
+    unsigned long long* status_ = nullptr;
+    uint32_t* sets_ = nullptr;  // 8 per virtual bird, debug only
+    StepCtl* ctl_ = nullptr;
+    float* radius_table_ = nullptr;
+    float* staging_ = nullptr;
+    size_t staging_cap_ = 0;
+
+    cudaGraphExec_t graph_ = nullptr;
+    uint32_t graph_steps_ = 0;
+};
+
+// Canonical bucket count for a flock of n birds (reference cuda/flock.cu:368-372).
+uint32_t buckets_for(uint32_t n);
+
+// Device-error and CUDA failures surface as this exception inside the library;
+// the C ABI turns it into a status code and a message.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+}  // namespace flk

@@ -1,0 +1,372 @@
+"""GPU parity: the sm_103a step through the C ABI against the CPU oracle.
+
+Bar (per step, from the same input state):
+  * cell keys, bucket offsets and the stable sorted order: bit-exact;
+  * the four neighbour sets of every deciding bird (R set, its r_h-excluded
+    cohesion subset, the blind-angle alignment subset, the 2R centrality set):
+    counts and order-independent hashes bit-exact;
+  * next_decision, neighbour count and the new radius: bit-exact;
+  * position and velocity: relative error <= 1e-5 per bird (vector norm),
+    and the reference tool's strict diff (max |dpos|, |dvel| <= 1e-3).
+Tolerances are written here, next to the checks.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5  # post-step pos/vel relative error bound
+
+
+def vec_rel(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Per-bird ||a - b|| / ||b|| (b the reference), floored at 1e-6 in the denominator."""
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-6)
+
+
+def one_step(native, oracle, w, time=0.0):
+    """Runs one GPU step (with grid + set outputs) and one oracle step."""
+    f = native.Flock(w, time)
+    dbg = f.step_debug()
+    t_gpu, g = f.read()
+    f.close()
+    t_cpu, c, sets, due = oracle.step(w, time)
+    keys, offs, srt = oracle.grid(w, native.buckets_for(len(w)))
+    return dict(t_gpu=t_gpu, g=g, dbg=dbg, t_cpu=t_cpu, c=c, sets=sets, due=due, keys=keys, offs=offs, srt=srt)
+
+
+def assert_step_parity(native, oracle, w, time=0.0, check_fp64=False):
+    r = one_step(native, oracle, w, time)
+    g, c, dbg = r["g"], r["c"], r["dbg"]
+    n = len(w)
+    assert r["t_gpu"] == r["t_cpu"]
+    # grid: bit-exact
+    assert np.array_equal(dbg["keys"], r["keys"]), "cell keys differ"
+    assert np.array_equal(dbg["offsets"], r["offs"]), "bucket offsets differ"
+    assert np.array_equal(dbg["sorted"], r["srt"]), "sorted order differs"
+    assert oracle.check_grid(dbg["keys"], dbg["offsets"], dbg["sorted"], native.buckets_for(n), w) == 0
+    # neighbour sets: bit-exact (zeros for birds that did not decide)
+    bad = np.nonzero(np.any(dbg["sets"] != r["sets"], axis=1))[0]
+    assert len(bad) == 0, f"{len(bad)} birds with different neighbour sets, first {bad[:5]}: " \
+                          f"gpu {dbg['sets'][bad[:1]]} cpu {r['sets'][bad[:1]]}"
+    # exact words
+    assert np.array_equal(g[:, 12], c[:, 12]), "next_decision"
+    assert np.array_equal(g[:, 13].view(np.uint32), c[:, 13].view(np.uint32)), "neighbour counts"
+    assert np.array_equal(g[:, 8], c[:, 8]), "radius"
+    # state: relative error
+    if n:
+        rp = vec_rel(g[:, 0:3], c[:, 0:3])
+        rv = vec_rel(g[:, 3:6], c[:, 3:6])
+        assert rp.max() <= REL_TOL, rp.max()
+        assert rv.max() <= REL_TOL, rv.max()
+        ok, maxes, mism, _ = oracle.diff(g, c)
+        assert ok and mism == 0, maxes
+        # steering / centrality: sums in a different order, rounding-level agreement
+        ds = np.abs(g[:, 9:12].astype(np.float64) - c[:, 9:12]).max()
+        assert ds <= 1e-5, ds
+        assert np.abs(g[:, 14].astype(np.float64) - c[:, 14]).max() <= 1e-5
+    if check_fp64 and n:
+        d = oracle.step_f64(w, time)
+        e_gpu = max(vec_rel(g[:, 0:3], d[:, 0:3]).max(), vec_rel(g[:, 3:6], d[:, 3:6]).max())
+        e_cpu = max(vec_rel(c[:, 0:3], d[:, 0:3]).max(), vec_rel(c[:, 3:6], d[:, 3:6]).max())
+        print(f"error vs FP64 step: gpu {e_gpu:.3e}  oracle {e_cpu:.3e}")
+        assert e_gpu <= REL_TOL
+    return r
+
+
+def bird(pos, vel=(10, 0, 0), radius=1.5, next_decision=0.0):
+    w = np.zeros(15, dtype=np.float32)
+    w[0:3] = pos
+    w[3:6] = vel
+    w[8] = radius
+    w[12] = next_decision
+    return w
+
+
+# ---- the benchmark scatter ---------------------------------------------------
+@pytest.mark.parametrize("n,seed", [(2000, 1), (100_000, 1), (50_000, 7)])
+def test_one_step_parity_generated(native, oracle, n, seed):
+    w = oracle.scatter(n, seed)
+    r = assert_step_parity(native, oracle, w, check_fp64=True)
+    assert r["due"].sum() > 0
+
+
+def test_one_step_parity_settled_state(native, oracle):
+    # a state 60 steps in: adapted radii, steering held, some roll
+    w = oracle.scatter(3000, 1)
+    t, w = oracle.steps(w, 0.0, 60)
+    assert_step_parity(native, oracle, w, time=t, check_fp64=True)
+
+
+def test_parity_ladder_2000(native, oracle):
+    """scripts/parity.sh: K = 1, 10, 30 strict; 100 with <= 2 outliers <= 1e-2;
+    1000 aggregate statdiff."""
+    w0 = oracle.scatter(2000, 1)
+    f = native.Flock(w0, 0.0)
+    t_cpu, c = 0.0, w0
+    done = 0
+    for k in (1, 10, 30, 100, 1000):
+        f.step(k - done)
+        t_cpu, c = oracle.steps(c, t_cpu, k - done)
+        done = k
+        t_gpu, g = f.read()
+        assert t_gpu == np.float32(t_cpu)
+        if k <= 30:
+            ok, maxes, mism, _ = oracle.diff(g, c)
+            assert ok, (k, maxes, mism)
+        elif k <= 100:
+            ok, maxes, mism, outl = oracle.diff(g, c, allow=2, outlier_max=1e-2)
+            assert ok, (k, maxes, mism, outl)
+        else:
+            ok, d = oracle.statdiff(g, c)
+            assert ok, (k, d)
+    f.close()
+
+
+# ---- hand-made edge cases ----------------------------------------------------
+def test_empty_flock(native):
+    f = native.Flock(np.zeros((0, 15), np.float32), 0.5)
+    f.step(3)
+    t, w = f.read()
+    assert w.shape == (0, 15)
+    assert t == np.float32(np.float32(np.float32(np.float32(0.5) + np.float32(0.005)) + np.float32(0.005)) +
+                           np.float32(0.005))
+    dbg = f.step_debug()
+    assert dbg["offsets"].max() == 0
+
+
+def test_single_and_pair(native, oracle):
+    assert_step_parity(native, oracle, bird((0, 0, 100))[None])
+    w = np.stack([bird((0, 0, 100), radius=2.0), bird((0, 0.5, 100), radius=2.0)])
+    r = assert_step_parity(native, oracle, w)
+    assert r["g"][0, 13].view(np.uint32) == 1 and r["g"][0, 10] < 0
+
+
+def test_boundaries_and_exact_radius(native, oracle):
+    # birds on cell faces/corners, pairs at exactly r and exactly 2r, negative cells
+    pts = [(4.0, 0.0, 100.0), (3.0, 0.0, 100.0), (5.0, 0.0, 100.0), (4.0, 4.0, 100.0), (0.0, 0.0, 100.0),
+           (-4.0, -4.0, 96.0), (-3.0, -4.0, 96.0), (-5.0, -4.0, 96.0), (8.0, 0.0, 100.0), (2.0, 0.0, 100.0),
+           (-0.0, 0.0, 104.0), (0.0, -1.0, 104.0), (12.0, 12.0, 112.0), (12.0, 12.0, 113.0), (13.0, 12.0, 112.0)]
+    w = np.stack([bird(p, radius=1.0) for p in pts])
+    w[3, 8] = 2.0
+    w[8, 3:6] = 0.0  # zero velocity: forward() fallback
+    assert_step_parity(native, oracle, w)
+
+
+def colliding_cells(mask: int, count: int = 2, near: bool = False):
+    """Finds distinct cells whose hash & mask coincide (within one 3x3x3
+    neighbourhood when near=True)."""
+    rng = np.random.default_rng(0)
+
+    def h(c):
+        c = np.asarray(c, dtype=np.int64).astype(np.uint32)
+        return ((c[..., 0] * np.uint32(73856093)) ^ (c[..., 1] * np.uint32(19349663)) ^
+                (c[..., 2] * np.uint32(83492791))) & np.uint32(mask)
+
+    if not near:
+        base = np.array([0, 0, 25])
+        cand = rng.integers(-200, 200, size=(400_000, 3))
+        hit = np.nonzero(h(cand) == h(base))[0]
+        return [base, cand[hit[0]]]
+    offs = np.array([(i, j, k) for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)])
+    for _ in range(200):
+        centres = rng.integers(-3000, 3000, size=(20_000, 3))
+        box = centres[:, None, :] + offs[None]
+        hb = h(box)
+        srt = np.sort(hb, axis=1)
+        dup = np.nonzero(np.any(srt[:, 1:] == srt[:, :-1], axis=1))[0]
+        if len(dup):
+            k = dup[0]
+            vals, cnt = np.unique(hb[k], return_counts=True)
+            v = vals[cnt > 1][0]
+            return [box[k][i] for i in np.nonzero(hb[k] == v)[0][:2]] + [centres[k]]
+    raise AssertionError("no colliding pair found")
+
+
+def test_hash_collisions(native, oracle):
+    mask = native.buckets_for(40) - 1
+    rng = np.random.default_rng(1)
+    birds = []
+    a, b = colliding_cells(mask)
+    for c in (a, b):
+        for _ in range(6):
+            birds.append(bird(c * 4.0 + rng.uniform(0.2, 3.8, 3), radius=1.8))
+    # two cells of one neighbourhood sharing a bucket: dedup must visit the bucket once
+    c1, c2, centre = colliding_cells(mask, near=True)
+    for c in (c1, c2, centre):
+        for _ in range(8):
+            birds.append(bird(c * 4.0 + rng.uniform(0.0, 4.0, 3), radius=1.9))
+    w = np.stack(birds).astype(np.float32)
+    r = assert_step_parity(native, oracle, w)
+    assert len(np.unique(r["keys"])) < len({tuple(np.floor(p / 4)) for p in w[:, :3]})
+
+
+def test_dense_cell_and_long_ranges(native, oracle):
+    # 300 birds in one 4 m cell: bucket range > 32 takes the counting sort path
+    rng = np.random.default_rng(2)
+    pos = rng.uniform(0.0, 4.0, size=(300, 3)) + np.array([40.0, 40.0, 100.0])
+    w = np.stack([bird(p, radius=0.6, next_decision=rng.uniform(0, 0.01)) for p in pos]).astype(np.float32)
+    assert_step_parity(native, oracle, w)
+
+
+def test_wide_radii_take_the_cell_walk_and_brute_force_paths(native, oracle):
+    w = oracle.scatter(4000, 11)
+    w[:200, 8] = 5.0    # 2R = 10 m: > 32 cells, cell walk with the exact cell check
+    w[200:210, 8] = 60.0  # 2R = 120 m covers the flock: brute force over the flock's range
+    w[:, 12] = 0.0      # everyone decides
+    assert_step_parity(native, oracle, w)
+
+
+def test_steps_are_deterministic(native):
+    w = native.generate(20_000, 3)
+    outs = []
+    for _ in range(2):
+        f = native.Flock(w)
+        f.step(12)
+        outs.append(f.read()[1])
+        f.close()
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+def test_graph_and_eager_launches_agree(native):
+    w = native.generate(30_000, 4)
+    a = native.Flock(w)
+    a.step(23)  # two 10-step graphs + 3 eager steps
+    b = native.Flock(w)
+    b.step_timed(23, 0)  # 23 eager steps with events
+    assert a.read()[1].tobytes() == b.read()[1].tobytes()
+    assert a.read()[0] == b.read()[0]
+
+
+def test_file_drop_in_and_cli(native, oracle, tmp_path):
+    import subprocess
+
+    src = str(tmp_path / "start.flk")
+    out = str(tmp_path / "end.flk")
+    ref = str(tmp_path / "ref.flk")
+    subprocess.run([oracle.CLI, "gen", "--birds", "2000", "--seed", "1", "--out", src], check=True)
+    r = subprocess.run([native.CLI_PATH, "--in", src, "--steps", "10", "--warmup", "2", "--out", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for name in ("grid_histogram", "grid_scan", "grid_scatter", "decide", "integrate", "step total",
+                 "bird-steps/s", "# 2000 birds, 10 steps (2 warm-up, not timed)"):
+        assert name in r.stdout
+    subprocess.run([oracle.CLI, "step", "--in", src, "--steps", "10", "--out", ref], check=True)
+    d = subprocess.run([oracle.CLI, "diff", ref, out], capture_output=True, text=True)
+    assert d.returncode == 0 and "neighbour-count mismatches 0 of 2000" in d.stdout, d.stdout
+
+
+# ---- full-size sizes: size-independent properties -----------------------------
+def test_one_million_grid_and_sampled_sets(native, oracle):
+    n = 1_000_000
+    w = native.generate(n, 1)
+    f = native.Flock(w)
+    dbg = f.step_debug()
+    _, g = f.read()
+    f.close()
+    B = native.buckets_for(n)
+    keys, offs, srt = oracle.grid(w, B)
+    assert np.array_equal(dbg["keys"], keys)
+    assert np.array_equal(dbg["offsets"], offs)
+    assert np.array_equal(dbg["sorted"], srt)
+    due = np.nonzero(dbg["sets"].any(axis=1))[0]
+    t = np.float32(np.float32(0.0) + np.float32(0.005))
+    want_due = np.nonzero(t >= w[:, 12])[0]
+    lone = want_due[~dbg["sets"][want_due].any(axis=1)]
+    # a deciding bird has an all-zero summary only if it found no neighbour at all
+    assert np.isin(due, want_due).all()
+    rng = np.random.default_rng(5)
+    sample = rng.choice(want_due, size=1500, replace=False)
+    sets, dec = oracle.decide_many(w, sample)
+    assert np.array_equal(dbg["sets"][sample], sets)
+    assert np.array_equal(g[sample, 8], dec[:, 3])  # radius
+    assert np.array_equal(g[sample, 13].view(np.uint32), dec[:, 4].view(np.uint32))
+    assert np.abs(g[sample, 9:12] - dec[:, 0:3]).max() <= 1e-5
+    # integrate of the sampled birds from their decided steering
+    pre = w[sample].copy()
+    pre[:, 9:12] = dec[:, 0:3]
+    post = oracle.integrate_all(pre)
+    assert vec_rel(g[sample, 0:3], post[:, 0:3]).max() <= REL_TOL
+    assert vec_rel(g[sample, 3:6], post[:, 3:6]).max() <= REL_TOL
+    assert len(lone) < 0.01 * len(want_due)
+
+
+# ---- batched and served --------------------------------------------------------
+def test_batched_flocks_equal_plain_runs(native):
+    sizes = [1000, 37, 0, 5000, 20_000, 1, 2500, 64_000]
+    flocks = [native.generate(n, 3 + k) for k, n in enumerate(sizes)]
+    b = native.Batch()
+    ids = [b.add(w) for w in flocks]
+    b.step(17)
+    for fid, w in zip(ids, flocks):
+        p = native.Flock(w)
+        p.step(17)
+        tp, wp = p.read()
+        tb, wb = b.read(fid)
+        assert tp == tb
+        assert wp.tobytes() == wb.tobytes(), f"flock of {len(w)} birds differs"
+        p.close()
+    b.close()
+
+
+def test_batched_debug_matches_oracle_per_flock(native, oracle):
+    sizes = [3000, 700, 12_000]
+    flocks = [oracle.scatter(n, 10 + k) for k, n in enumerate(sizes)]
+    b = native.Batch()
+    ids = [b.add(w) for w in flocks]
+    dbgs = b.step_debug(ids[::-1])[::-1]
+    for fid, w, dbg in zip(ids, flocks, dbgs):
+        keys, offs, srt = oracle.grid(w)
+        assert np.array_equal(dbg["keys"], keys) and np.array_equal(dbg["offsets"], offs)
+        assert np.array_equal(dbg["sorted"], srt)
+        _, c, sets, _ = oracle.step(w, 0.0)
+        assert np.array_equal(dbg["sets"], sets)
+        _, g = b.read(fid)
+        assert vec_rel(g[:, 0:3], c[:, 0:3]).max() <= REL_TOL
+    b.close()
+
+
+def test_batched_uneven_step_counts(native):
+    sizes = [4000, 900, 15_000]
+    flocks = [native.generate(n, 20 + k) for k, n in enumerate(sizes)]
+    steps = [3, 25, 11]
+    b = native.Batch()
+    ids = [b.add(w) for w in flocks]
+    b.step_each(ids, steps)
+    for fid, w, k in zip(ids, flocks, steps):
+        p = native.Flock(w)
+        p.step(k)
+        assert p.read()[1].tobytes() == b.read(fid)[1].tobytes()
+        assert p.read()[0] == b.read(fid)[0]
+        p.close()
+    b.close()
+
+
+def test_served_results_equal_alone_and_in_the_mix(native):
+    rng = np.random.default_rng(5)
+    reqs = [(int(n), int(s)) for n, s in zip(rng.integers(500, 30_000, 10), rng.integers(3, 40, 10))]
+    states = [native.generate(n, 100 + k) for k, (n, _) in enumerate(reqs)]
+    with native.Pool(budget_bytes=native.bytes_for(60_000), chunk_steps=4) as pool:
+        tickets = [pool.submit(w, s) for w, (_, s) in zip(states, reqs)]
+        results = [pool.wait(t) for t in tickets]
+        st = pool.stats()
+    assert st["completed"] == len(reqs)
+    for (n, s), w, (t, out, lat) in zip(reqs, states, results):
+        p = native.Flock(w)
+        p.step(s)
+        tp, wp = p.read()
+        assert tp == t and wp.tobytes() == out.tobytes(), (n, s)
+        assert lat > 0
+        p.close()
+
+
+def test_pool_rejects_a_request_over_budget(native):
+    with native.Pool(budget_bytes=native.bytes_for(1000), chunk_steps=5) as pool:
+        with pytest.raises(native.FlockError) as e:
+            pool.submit(native.generate(50_000, 1), 3)
+        assert e.value.code == -8
+        t = pool.submit(native.generate(800, 1), 0)  # zero steps completes at once
+        assert pool.wait(t)[0] == 0.0
