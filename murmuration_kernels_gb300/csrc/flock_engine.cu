@@ -907,8 +907,11 @@ std::vector<int> Engine::flock_ids() const {
 }
 
 void Engine::sync_times() {
-    // the device table holds the live clocks of the flocks in it
-    if (table_h_.empty() || !table_d_) return;
+    // The device table holds the live clocks and countdowns once steps have
+    // run; until then the host copy is authoritative (it may hold step counts
+    // set since the last run that the device has not seen yet).
+    if (!device_ahead_ || table_h_.empty() || !table_d_) return;
+    device_ahead_ = false;
     std::vector<FlockDesc> t(table_h_.size());
     FLK_CUDA(cudaMemcpyAsync(t.data(), table_d_, t.size() * sizeof(FlockDesc), cudaMemcpyDeviceToHost, stream_));
     FLK_CUDA(cudaStreamSynchronize(stream_));
@@ -1054,6 +1057,7 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     FLK_CUDA(e);
     std::vector<cudaEvent_t> ev(2 * (size_t)steps);
     for (auto& x : ev) FLK_CUDA(cudaEventCreate(&x));
+    device_ahead_ = true;
     for (uint32_t s = 0; s < steps; ++s) {
         if (n16) k_flush<<<num_sms_ * 4, 256, 0, stream_>>>(flush, n16, s);
         FLK_CUDA(cudaEventRecord(ev[2 * s], stream_));
@@ -1113,6 +1117,7 @@ void Engine::rebuild_table() {
     if (!same_shape) free_graphs();
     ensure_scratch();
     table_dirty_ = false;
+    device_ahead_ = false;  // the device table now equals the host copy
 }
 
 void Engine::ensure_scratch() {
@@ -1154,6 +1159,7 @@ static int pgrid(int sms, int per_sm, uint64_t items, uint64_t per_cta) {
 }
 
 void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
+    device_ahead_ = true;
     const int nfl = (int)table_h_.size();
     const int sblocks = pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256);
     const uint32_t ntiles = Btot_ / SCAN_TILE;
@@ -1203,6 +1209,7 @@ void Engine::run(uint32_t steps) {
     uint32_t done = 0;
     if (steps >= chunk) {
         ensure_graph();
+        device_ahead_ = true;
         for (; done + chunk <= steps; done += chunk) FLK_CUDA(cudaGraphLaunch(graph_, stream_));
     }
     for (; done < steps; ++done) enqueue_step(false);

@@ -146,6 +146,7 @@ private:
 
     // flock table of flocks with remaining > 0, in slot order
     bool table_dirty_ = true;
+    bool device_ahead_ = false;  // steps ran since the host last read the device table
     std::vector<FlockDesc> table_h_;
     std::vector<int> table_ids_;
     FlockDesc* table_d_ = nullptr;

@@ -1,0 +1,208 @@
+#!/usr/bin/env python3
+"""Generates golden fixtures from the REFERENCE's own CUDA kernels.
+
+The reference's cuda/flock.cu is compiled unchanged for sm_103a into
+oracle/_ref/flock_ref_sm103a.cubin (oracle/Makefile, target `ref`, run where the
+reference project is mounted). This script loads that cubin with the CUDA
+driver API and drives its kernels exactly as the reference's host loop does
+(cuda/flock.cu:403-470: buckets_for, memset, grid_histogram, the three scan
+kernels, grid_scatter, decide, integrate, one stream, time += DT in f32 on the
+host), on the reference generator's starting states. It writes:
+
+  ref_cuda_2000_s1.npz     2000 birds, seed 1 (scripts/parity.sh's case):
+                           input, state after 1 and after 100 steps, and the
+                           first step's bucket keys and offsets
+  ref_cuda_100k_s1.npz     100,000 birds, seed 1, one step: SHA-256 digests of
+                           the bucket keys, offsets and neighbour counts, plus
+                           every 97th bird's full state
+
+Run on a machine with a GPU (the fixtures are committed; tests only read them):
+    python tests/golden/make_reference_fixtures.py OUTDIR
+
+Safety: before any launch it checks each kernel's parameter layout with
+cuFuncGetParamInfo against the struct built here, and aborts on a mismatch.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+CUBIN = os.path.join(ROOT, "oracle", "_ref", "flock_ref_sm103a.cubin")
+
+DT = np.float32(0.005)
+SCAN_BLOCK = 2048  # cuda/flock.cu:113-115
+
+
+class FlockArg(C.Structure):
+    """cuda/flock.cu:93-111, passed by value to every kernel."""
+    _fields_ = [("n", C.c_int), ("buckets", C.c_uint32)] + [
+        (k, C.c_uint64) for k in ("pos", "vel", "steer", "roll", "spin", "radius", "next_decision", "centrality",
+                                  "neighbours", "bucket", "counts", "offsets", "block_sums", "sorted")]
+
+
+class Driver:
+    def __init__(self):
+        self.cu = C.CDLL("libcuda.so.1")
+        self.ck(self.cu.cuInit(0))
+        dev = C.c_int()
+        self.ck(self.cu.cuDeviceGet(C.byref(dev), 0))
+        self.ctx = C.c_void_p()
+        self.ck(self.cu.cuDevicePrimaryCtxRetain(C.byref(self.ctx), dev))
+        self.ck(self.cu.cuCtxSetCurrent(self.ctx))
+        self.mod = C.c_void_p()
+        self.ck(self.cu.cuModuleLoad(C.byref(self.mod), CUBIN.encode()))
+        self.allocs = []
+
+    def ck(self, rc):
+        if rc != 0:
+            name = C.c_char_p()
+            self.cu.cuGetErrorName(rc, C.byref(name))
+            raise RuntimeError(f"CUDA driver error {rc} {name.value}")
+
+    def fn(self, mangled: str, sizes: list[int]):
+        f = C.c_void_p()
+        self.ck(self.cu.cuModuleGetFunction(C.byref(f), self.mod, mangled.encode()))
+        off, size = C.c_size_t(), C.c_size_t()
+        for i, want in enumerate(sizes):
+            self.ck(self.cu.cuFuncGetParamInfo(f, C.c_size_t(i), C.byref(off), C.byref(size)))
+            if size.value != want:
+                raise RuntimeError(f"{mangled}: parameter {i} is {size.value} bytes, expected {want}")
+        if self.cu.cuFuncGetParamInfo(f, C.c_size_t(len(sizes)), C.byref(off), C.byref(size)) == 0:
+            raise RuntimeError(f"{mangled}: more parameters than expected")
+        return f
+
+    def alloc(self, nbytes: int) -> int:
+        p = C.c_uint64()
+        self.ck(self.cu.cuMemAlloc_v2(C.byref(p), C.c_size_t(max(nbytes, 4))))
+        self.allocs.append(p.value)
+        return p.value
+
+    def h2d(self, dst: int, a: np.ndarray):
+        a = np.ascontiguousarray(a)
+        self.ck(self.cu.cuMemcpyHtoD_v2(C.c_uint64(dst), a.ctypes.data_as(C.c_void_p), C.c_size_t(a.nbytes)))
+
+    def d2h(self, a: np.ndarray, src: int):
+        self.ck(self.cu.cuMemcpyDtoH_v2(a.ctypes.data_as(C.c_void_p), C.c_uint64(src), C.c_size_t(a.nbytes)))
+
+    def zero(self, dst: int, words: int):
+        self.ck(self.cu.cuMemsetD32_v2(C.c_uint64(dst), C.c_uint(0), C.c_size_t(words)))
+
+    def launch(self, f, grid: int, block: int, args: list):
+        ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        self.ck(self.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, 0, None, ptrs, None))
+
+    def sync(self):
+        self.ck(self.cu.cuCtxSynchronize())
+
+    def free(self):
+        for p in self.allocs:
+            self.cu.cuMemFree_v2(C.c_uint64(p))
+        self.allocs = []
+
+
+def buckets_for(n: int) -> int:  # cuda/flock.cu:368-372
+    want = 1
+    while want < n * 2:
+        want <<= 1
+    return min(max(want, 1 << 16), 1 << 22)
+
+
+def run_reference(drv: Driver, words: np.ndarray, time: float, steps: int):
+    """The reference's main(): upload (flock.cu:414-437), step loop (453-470),
+    download (494-519). Returns (time, words, keys of step 1, offsets of step 1)."""
+    n = len(words)
+    B = buckets_for(n)
+    szF = C.sizeof(FlockArg)
+    k_hist = drv.fn("_Z14grid_histogram5Flock", [szF])
+    k_sblk = drv.fn("_Z16grid_scan_blocks5Flock", [szF])
+    k_stot = drv.fn("_Z16grid_scan_totals5Flockj", [szF, 4])
+    k_sadd = drv.fn("_Z13grid_scan_add5Flock", [szF])
+    k_scat = drv.fn("_Z12grid_scatter5Flock", [szF])
+    k_dec = drv.fn("_Z6decide5Flockf", [szF, 4])
+    k_int = drv.fn("_Z9integrate5Flock", [szF])
+    f = FlockArg()
+    f.n, f.buckets = n, B
+    for k in ("pos", "vel", "steer"):
+        setattr(f, k, drv.alloc(n * 16))
+    for k in ("roll", "spin", "radius", "next_decision", "centrality", "neighbours", "bucket", "sorted"):
+        setattr(f, k, drv.alloc(n * 4))
+    f.counts = drv.alloc(B * 4)
+    f.offsets = drv.alloc((B + 1) * 4)
+    f.block_sums = drv.alloc((B // SCAN_BLOCK) * 4)
+    w = words.astype(np.float32)
+    f4 = lambda cols: np.concatenate([w[:, cols], np.zeros((n, 1), np.float32)], axis=1)
+    drv.h2d(f.pos, f4([0, 1, 2]))
+    drv.h2d(f.vel, f4([3, 4, 5]))
+    drv.h2d(f.steer, f4([9, 10, 11]))
+    for k, col in (("roll", 6), ("spin", 7), ("radius", 8), ("next_decision", 12), ("neighbours", 13),
+                   ("centrality", 14)):
+        drv.h2d(getattr(f, k), np.ascontiguousarray(w[:, col]))
+    TB = 256
+    blocks = (n + TB - 1) // TB
+    scan_blocks = C.c_uint32(B // SCAN_BLOCK)
+    t = np.float32(time)
+    keys1 = offs1 = None
+    for s in range(steps):
+        t = np.float32(t + DT)
+        drv.zero(f.counts, B)
+        drv.launch(k_hist, blocks, TB, [f])
+        drv.launch(k_sblk, B // SCAN_BLOCK, 256, [f])
+        drv.launch(k_stot, 1, 256, [f, scan_blocks])
+        drv.launch(k_sadd, (B + TB - 1) // TB, TB, [f])
+        drv.launch(k_scat, blocks, TB, [f])
+        drv.launch(k_dec, blocks, TB, [f, C.c_float(float(t))])
+        drv.launch(k_int, blocks, TB, [f])
+        if s == 0:
+            drv.sync()
+            keys1 = np.zeros(n, np.uint32)
+            offs1 = np.zeros(B + 1, np.uint32)
+            drv.d2h(keys1, f.bucket)
+            drv.d2h(offs1, f.offsets)
+    drv.sync()
+    out = np.zeros((n, 15), np.float32)
+    tmp4 = np.zeros((n, 4), np.float32)
+    for k, cols in (("pos", [0, 1, 2]), ("vel", [3, 4, 5]), ("steer", [9, 10, 11])):
+        drv.d2h(tmp4, getattr(f, k))
+        out[:, cols] = tmp4[:, :3]
+    tmp = np.zeros(n, np.float32)
+    for k, col in (("roll", 6), ("spin", 7), ("radius", 8), ("next_decision", 12), ("neighbours", 13),
+                   ("centrality", 14)):
+        drv.d2h(tmp, getattr(f, k))
+        out[:, col] = tmp
+    drv.free()
+    return float(t), out, keys1, offs1
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def main(outdir: str):
+    from oracle import pyoracle as o
+
+    os.makedirs(outdir, exist_ok=True)
+    drv = Driver()
+    w = o.scatter(2000, 1)
+    t1, out1, keys1, offs1 = run_reference(drv, w, 0.0, 1)
+    t100, out100, _, _ = run_reference(drv, w, 0.0, 100)
+    np.savez_compressed(os.path.join(outdir, "ref_cuda_2000_s1.npz"), input=w, time1=np.float32(t1), out1=out1,
+                        keys1=keys1, offsets1=offs1, time100=np.float32(t100), out100=out100)
+    w = o.scatter(100_000, 1)
+    t, out, keys, offs = run_reference(drv, w, 0.0, 1)
+    pick = np.arange(0, 100_000, 97)
+    np.savez_compressed(os.path.join(outdir, "ref_cuda_100k_s1.npz"), time1=np.float32(t), pick=pick,
+                        out1_pick=out[pick], keys_sha=sha(keys), offsets_sha=sha(offs),
+                        neighbours_sha=sha(out[:, 13].view(np.uint32)),
+                        next_decision_sha=sha(out[:, 12]))
+    print("wrote fixtures to", outdir)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)

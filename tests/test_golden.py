@@ -1,0 +1,108 @@
+"""Golden fixtures produced by the REFERENCE's own CUDA kernels (cuda/flock.cu
+compiled unchanged for sm_103a and driven by tests/golden/make_reference_fixtures.py
+on a GB300). They pin the oracle (CPU tests) and the product (GPU tests).
+
+The reference logged these figures for its CUDA backend against its Rust
+oracle at 2000 birds (docs/results/rtx4000ada-2026-10-21/logs/cuda-parity-1.log,
+cuda-parity-100.log): after 1 step max |dpos| 4.768e-7, |dvel| 9.537e-7,
+|dcentrality| 1.192e-7, 0 neighbour mismatches; after 100 steps 7.629e-6, 0.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+# ---- the oracle against the reference kernels (CPU) -------------------------
+def test_generator_matches_the_reference_input(oracle):
+    z = load("ref_cuda_2000_s1.npz")
+    assert z["input"].tobytes() == oracle.scatter(2000, 1).tobytes()
+
+
+def test_oracle_grid_equals_reference_kernels(oracle):
+    z = load("ref_cuda_2000_s1.npz")
+    keys, offs, _ = oracle.grid(z["input"])
+    assert np.array_equal(keys, z["keys1"])
+    assert np.array_equal(offs, z["offsets1"])
+
+
+def test_oracle_one_step_equals_reference_kernels(oracle):
+    z = load("ref_cuda_2000_s1.npz")
+    t, c, _, _ = oracle.step(z["input"], 0.0)
+    assert np.float32(t) == z["time1"]
+    ok, maxes, mism, _ = oracle.diff(c, z["out1"])
+    assert ok and mism == 0
+    # the reference's own logged 1-step figures (cuda-parity-1.log:2-3)
+    assert maxes[0] <= 4.768e-7 * 1.001 and maxes[1] <= 9.537e-7 * 1.001 and maxes[3] <= 1.192e-7 * 1.001
+    assert np.array_equal(c[:, 12], z["out1"][:, 12])
+    assert np.array_equal(c[:, 8], z["out1"][:, 8])
+
+
+def test_oracle_hundred_steps_equals_reference_kernels(oracle):
+    z = load("ref_cuda_2000_s1.npz")
+    t, c = oracle.steps(z["input"], 0.0, 100)
+    assert np.float32(t) == z["time100"]
+    ok, maxes, mism, _ = oracle.diff(c, z["out100"])
+    assert ok and mism == 0
+    assert maxes[0] <= 7.629e-6 * 1.01  # cuda-parity-100.log:2
+
+
+def test_oracle_100k_grid_and_counts_equal_reference_kernels(oracle):
+    z = load("ref_cuda_100k_s1.npz")
+    w = oracle.scatter(100_000, 1)
+    keys, offs, _ = oracle.grid(w)
+    assert sha(keys) == str(z["keys_sha"])
+    assert sha(offs) == str(z["offsets_sha"])
+    t, c, _, _ = oracle.step(w, 0.0)
+    assert sha(c[:, 13].view(np.uint32)) == str(z["neighbours_sha"])
+    assert sha(c[:, 12]) == str(z["next_decision_sha"])
+    pick = z["pick"]
+    ok, maxes, mism, _ = oracle.diff(c[pick], z["out1_pick"])
+    assert ok and mism == 0, maxes
+
+
+# ---- the product against the reference kernels (GPU) ------------------------
+@pytest.mark.gpu
+def test_product_equals_reference_kernels_2000(native, oracle):
+    z = load("ref_cuda_2000_s1.npz")
+    f = native.Flock(z["input"], 0.0)
+    dbg = f.step_debug()
+    t1, g1 = f.read()
+    f.step(99)
+    t100, g100 = f.read()
+    f.close()
+    assert np.array_equal(dbg["keys"], z["keys1"]) and np.array_equal(dbg["offsets"], z["offsets1"])
+    assert np.float32(t1) == z["time1"] and np.float32(t100) == z["time100"]
+    ok, maxes, mism, _ = oracle.diff(g1, z["out1"])
+    assert ok and mism == 0, maxes
+    assert np.array_equal(g1[:, 13].view(np.uint32), z["out1"][:, 13].view(np.uint32))
+    ok, maxes, mism, _ = oracle.diff(g100, z["out100"], allow=2, outlier_max=1e-2)
+    assert ok, (maxes, mism)
+
+
+@pytest.mark.gpu
+def test_product_equals_reference_kernels_100k(native, oracle):
+    z = load("ref_cuda_100k_s1.npz")
+    w = oracle.scatter(100_000, 1)
+    f = native.Flock(w, 0.0)
+    dbg = f.step_debug()
+    _, g = f.read()
+    f.close()
+    assert sha(dbg["keys"]) == str(z["keys_sha"]) and sha(dbg["offsets"]) == str(z["offsets_sha"])
+    assert sha(g[:, 13].view(np.uint32)) == str(z["neighbours_sha"])
+    assert sha(g[:, 12]) == str(z["next_decision_sha"])
+    ok, maxes, mism, _ = oracle.diff(g[z["pick"]], z["out1_pick"])
+    assert ok and mism == 0, maxes
