@@ -47,6 +47,7 @@ def commands(verbose_ptxas: bool = False) -> tuple[list[list[str]], list[list[st
     inc = os.path.join(ch, "include")
     os.makedirs(OUT, exist_ok=True)
     eng_o = os.path.join(OUT, "flock_engine.o")
+    noalloc_o = os.path.join(OUT, "flock_noalloc.o")
     abi_o = os.path.join(OUT, "flock_abi.o")
     lib = os.path.join(OUT, "libflock_gb300.so")
     cli = os.path.join(OUT, "flock_gb300")
@@ -54,13 +55,14 @@ def commands(verbose_ptxas: bool = False) -> tuple[list[list[str]], list[list[st
           "-c", os.path.join(CSRC, "flock_engine.cu"), "-o", eng_o]
     if verbose_ptxas:
         cu.insert(1, "-Xptxas=-v")
+    cu_na = cu[:cu.index("-c")] + ["-c", os.path.join(CSRC, "flock_noalloc.cu"), "-o", noalloc_o]
     cxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + inc,
            "-c", os.path.join(CSRC, "flock_abi.cpp"), "-o", abi_o]
-    link = [nvcc, ARCH, "-shared", "-o", lib, eng_o, abi_o, "-Xcompiler", "-fPIC", "-lpthread"]
+    link = [nvcc, ARCH, "-shared", "-o", lib, eng_o, noalloc_o, abi_o, "-Xcompiler", "-fPIC", "-lpthread"]
     cli_cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + inc, os.path.join(CSRC, "flock_cli.cpp"),
                "-o", cli, "-L" + OUT, "-lflock_gb300", "-L" + os.path.join(ch, "lib64"), "-lcudart",
                "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(ch, "lib64")]
-    return [cu, cxx], [link, cli_cmd]
+    return [cu, cu_na, cxx], [link, cli_cmd]
 
 
 def build(verbose_ptxas: bool = False) -> str:

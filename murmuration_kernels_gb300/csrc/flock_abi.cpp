@@ -88,6 +88,11 @@ int write_flk(const char* path, float time, const float* words, uint32_t n) {
 
 }  // namespace
 
+namespace flk {
+// Lets entry points defined in other translation units report through flk_last_error().
+__attribute__((visibility("hidden"))) void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace flk
+
 // ---------------------------------------------------------------------------
 // plain single flock
 // ---------------------------------------------------------------------------
