@@ -55,6 +55,9 @@ def commands(verbose_ptxas: bool = False) -> tuple[list[list[str]], list[list[st
           "-c", os.path.join(CSRC, "flock_engine.cu"), "-o", eng_o]
     if verbose_ptxas:
         cu.insert(1, "-Xptxas=-v")
+    # extra nvcc flags for launch-shape experiments, e.g. FLK_NVCC_FLAGS=-DFLK_DECIDE_MIN_BLOCKS=3
+    extra = os.environ.get("FLK_NVCC_FLAGS", "").split()
+    cu[1:1] = extra
     cu_na = cu[:cu.index("-c")] + ["-c", os.path.join(CSRC, "flock_noalloc.cu"), "-o", noalloc_o]
     cxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + inc,
            "-c", os.path.join(CSRC, "flock_abi.cpp"), "-o", abi_o]

@@ -1,0 +1,105 @@
+// Device helpers shared by the step's passes: f32 vector arithmetic with
+// explicit round-to-nearest operations (no FMA contraction), the reference's
+// forward/side/body_up (crates/flock-ref/src/model.rs:15-38), the cell hash
+// (cuda/flock.cu:77-83), warp utilities and relaxed loads/stores.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "flock_engine.h"
+#include "flock_params.h"
+
+namespace flk {
+
+constexpr uint32_t FULL = 0xFFFFFFFFu;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 buckets per tile
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;             // look-back polls before giving up
+constexpr uint32_t FLAG_A = 1u, FLAG_P = 2u;
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 add(f3 a, f3 b) { return mk(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 sub(f3 a, f3 b) { return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 mul(f3 a, float s) { return mk(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)); }
+__device__ __forceinline__ f3 dvs(f3 a, float s) { return mk(__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)); }
+__device__ __forceinline__ float dot(f3 a, f3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+// glam Vec3::cross
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return mk(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(b.y, a.z)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(b.z, a.x)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(b.x, a.y)));
+}
+__device__ __forceinline__ float len(f3 a) { return __fsqrt_rn(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) { return mul(a, __fdiv_rn(1.0f, len(a))); }
+__device__ __forceinline__ f3 normalize_or_zero(f3 a) {
+    const float rcp = __fdiv_rn(1.0f, len(a));
+    return (isfinite(rcp) && rcp > 0.0f) ? mul(a, rcp) : mk(0.f, 0.f, 0.f);
+}
+// f32::clamp (NaN passes through)
+__device__ __forceinline__ float clampf(float v, float lo, float hi) {
+    if (v < lo) v = lo;
+    if (v > hi) v = hi;
+    return v;
+}
+// model.rs:15-38
+__device__ __forceinline__ f3 forward(f3 v) { return dot(v, v) > 1e-12f ? normalize(v) : mk(1.f, 0.f, 0.f); }
+__device__ __forceinline__ f3 side_of(f3 f) {
+    const f3 s = cross(f, mk(0.f, 0.f, 1.f));
+    return dot(s, s) > 1e-8f ? normalize(s) : mk(1.f, 0.f, 0.f);
+}
+__device__ __forceinline__ f3 body_up(f3 f, float beta) {
+    const f3 side = side_of(f);
+    const f3 up0 = cross(side, f);
+    return add(mul(up0, cosf(beta)), mul(side, sinf(beta)));
+}
+__device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// cuda/flock.cu:77-83: cell = floor(p / 4), bucket = spatial hash & mask.
+__device__ __forceinline__ int cell1(float x) { return (int)floorf(__fmul_rn(x, INV_CELL)); }
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
+    return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ int find_flock_v(const FlockDesc* __restrict__ fl, int nfl, uint32_t v) {
+    int lo = 0, hi = nfl - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&fl[mid].vbase) <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int find_flock_b(const FlockDesc* __restrict__ fl, int nfl, uint32_t b) {
+    int lo = 0, hi = nfl - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&fl[mid].bbase) <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+
+}  // namespace flk

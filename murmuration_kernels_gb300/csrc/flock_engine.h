@@ -157,7 +157,7 @@ private:
     uint32_t scratch_V_ = 0, scratch_B_ = 0;
     uint32_t *key_ = nullptr, *arrival_ = nullptr, *tmp_ = nullptr, *sorted_ = nullptr, *occ_ = nullptr;
     uint2* due_ = nullptr;
-    float4 *spos_ = nullptr, *sfwd_ = nullptr;
+    float4 *spos_ = nullptr, *sfwd_ = nullptr;  // cell-ordered view read by decide
     uint32_t *counts_ = nullptr, *offsets_ = nullptr;
     unsigned long long* status_ = nullptr;
     uint32_t* sets_ = nullptr;  // 8 per virtual bird, debug only

@@ -1,0 +1,294 @@
+// Passes 1-4 of the step: .flk words <-> arena, cell key + histogram, the
+// single-pass decoupled look-back scan, scatter by arrival rank, and the
+// per-bucket stable sort that writes the cell-ordered view and the
+// deciding-bird list (reference cuda/flock.cu:118-179, made stable).
+#pragma once
+
+#include "device_common.cuh"
+
+namespace flk {
+
+// ---------------------------------------------------------------------------
+// .flk words <-> arena (A = pos,roll  B = vel,spin  C = steer,radius  D = next,nb,cen)
+// ---------------------------------------------------------------------------
+__global__ void k_unpack(const float* __restrict__ w, uint32_t n, uint32_t sbase, float4* A, float4* B, float4* C,
+                         float4* D) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* r = w + (size_t)i * WORDS;
+        const uint32_t s = sbase + i;
+        A[s] = make_float4(r[0], r[1], r[2], r[6]);
+        B[s] = make_float4(r[3], r[4], r[5], r[7]);
+        C[s] = make_float4(r[9], r[10], r[11], r[8]);
+        D[s] = make_float4(r[12], r[13], r[14], 0.f);
+    }
+}
+
+__global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t sbase, const float4* A, const float4* B,
+                       const float4* C, const float4* D) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float* r = w + (size_t)i * WORDS;
+        const uint32_t s = sbase + i;
+        const float4 a = A[s], b = B[s], c = C[s], d = D[s];
+        r[0] = a.x; r[1] = a.y; r[2] = a.z;
+        r[3] = b.x; r[4] = b.y; r[5] = b.z;
+        r[6] = a.w; r[7] = b.w; r[8] = c.w;
+        r[9] = c.x; r[10] = c.y; r[11] = c.z;
+        r[12] = d.x; r[13] = d.y; r[14] = d.z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pass 1: cell key + histogram (warp-aggregated atomics)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                                    const float4* __restrict__ A, uint32_t* __restrict__ key,
+                                                    uint32_t* __restrict__ arrival, uint32_t* __restrict__ counts,
+                                                    uint32_t* __restrict__ occ, StepCtl* __restrict__ ctl) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < V; v0 += stride) {
+        const uint32_t v = v0 + lane;
+        bool act = false;
+        uint32_t b = 0;
+        if (v < V) {
+            const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
+            if (__ldg(&d->remaining)) {
+                const float4 p = A[__ldg(&d->sbase) + (v - __ldg(&d->vbase))];
+                b = __ldg(&d->bbase) + (cell_hash(cell1(p.x), cell1(p.y), cell1(p.z)) & (__ldg(&d->buckets) - 1u));
+                key[v] = b;
+                act = true;
+            }
+        }
+        const uint32_t m = __ballot_sync(FULL, act);
+        if (act) {
+            const uint32_t peers = __match_any_sync(m, b);
+            const int leader = __ffs(peers) - 1;
+            uint32_t old = 0;
+            if ((int)lane == leader) old = atomicAdd(&counts[b], (uint32_t)__popc(peers));
+            old = __shfl_sync(m, old, leader);
+            const uint32_t rank = old + __popc(peers & lanemask_lt());
+            arrival[v] = rank;
+            const bool first = rank == 0;
+            const uint32_t fm = __ballot_sync(m, first);
+            if (fm) {
+                const int wl = __ffs(m) - 1;
+                uint32_t base = 0;
+                if ((int)lane == wl) base = atomicAdd(&ctl->occ_count, (uint32_t)__popc(fm));
+                base = __shfl_sync(m, base, wl);
+                if (first) occ[base + __popc(fm & lanemask_lt())] = b;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pass 2: single-pass decoupled look-back exclusive scan (counts -> offsets)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long scan_word(uint32_t epoch, uint32_t flag, uint32_t value) {
+    return ((unsigned long long)(epoch & 0x3FFFFFFFu) << 34) | ((unsigned long long)flag << 32) | value;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
+                                                       uint32_t ntiles, unsigned long long* __restrict__ status,
+                                                       StepCtl* __restrict__ ctl) {
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->scan_ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) {  // only after an aborted step left the ticket counter off
+        if (threadIdx.x == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+        return;
+    }
+    const uint32_t epoch = *(volatile uint32_t*)&ctl->epoch & 0x3FFFFFFFu;
+    const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+
+    uint4 c[SCAN_ITEMS / 4];
+    uint4* src = reinterpret_cast<uint4*>(counts + base);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; ++k) c[k] = src[k];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; ++k) src[k] = make_uint4(0, 0, 0, 0);  // histogram ready for next step
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; ++k) sum += c[k].x + c[k].y + c[k].z + c[k].w;
+
+    // block exclusive scan of the per-thread sums
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, inc, o);
+        if ((int)lane >= o) inc += y;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    uint32_t wpre = 0, agg = 0;
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; ++w) {
+        const uint32_t t = s_warp[w];
+        if (w < (int)warp) wpre += t;
+        agg += t;
+    }
+    const uint32_t texcl = wpre + inc - sum;
+
+    if (warp == 0) {
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_relaxed(&status[0], scan_word(epoch, FLAG_P, agg));
+        } else {
+            if (lane == 0) st_relaxed(&status[tile], scan_word(epoch, FLAG_A, agg));
+            int pred = (int)tile - 1;
+            uint32_t polls = 0;
+            while (true) {
+                const int idx = pred - (int)lane;
+                uint32_t flag = FLAG_P, val = 0;
+                while (true) {
+                    if (idx >= 0) {
+                        const unsigned long long w = ld_relaxed(&status[idx]);
+                        const bool ok = (uint32_t)(w >> 34) == epoch;
+                        flag = ok ? (uint32_t)((w >> 32) & 3u) : 0u;
+                        val = (uint32_t)w;
+                    }
+                    if (__all_sync(FULL, flag != 0)) break;
+                    if (++polls > SCAN_SPIN_LIMIT) {  // give up: record and let every waiter finish
+                        if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_SCAN_TIMEOUT);
+                        flag = FLAG_P;
+                        val = 0;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                const uint32_t pm = __ballot_sync(FULL, flag == FLAG_P);
+                const int firstp = pm ? __ffs(pm) - 1 : 32;
+                uint32_t x = ((int)lane <= firstp) ? val : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+                excl += x;
+                if (pm) break;
+                pred -= 32;
+            }
+            if (lane == 0) st_relaxed(&status[tile], scan_word(epoch, FLAG_P, excl + agg));
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + texcl;
+    uint4* dst = reinterpret_cast<uint4*>(offsets + base);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; ++k) {
+        uint4 o;
+        o.x = run; run += c[k].x;
+        o.y = run; run += c[k].y;
+        o.z = run; run += c[k].z;
+        o.w = run; run += c[k].w;
+        dst[k] = o;
+    }
+    if (tile == ntiles - 1 && threadIdx.x == SCAN_THREADS - 1) offsets[(size_t)ntiles * SCAN_TILE] = run;
+}
+
+// ---------------------------------------------------------------------------
+// pass 3: scatter by arrival rank
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                                 const uint32_t* __restrict__ key, const uint32_t* __restrict__ arrival,
+                                                 const uint32_t* __restrict__ offsets, uint32_t* __restrict__ tmp,
+                                                 StepCtl* __restrict__ ctl) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
+        if (!__ldg(&d->remaining)) continue;
+        const uint32_t pos = __ldg(&offsets[key[v]]) + arrival[v];
+        if (pos < V) tmp[pos] = v;
+        else atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pass 4: per-bucket stable order + cell-ordered view + deciding-bird list
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t bitonic32(uint32_t x, uint32_t lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t y = __shfl_xor_sync(FULL, x, j);
+            const bool up = (lane & k) == 0;
+            const bool lower = (lane & j) == 0;
+            x = (lower == up) ? min(x, y) : max(x, y);
+        }
+    }
+    return x;
+}
+
+__device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, const FlockDesc& d, int f, float t_now,
+                                            uint32_t lane, const float4* __restrict__ A, const float4* __restrict__ B,
+                                            const float4* __restrict__ D, uint32_t* __restrict__ sorted,
+                                            float4* __restrict__ spos, float4* __restrict__ sfwd,
+                                            uint2* __restrict__ due, StepCtl* __restrict__ ctl) {
+    bool is_due = false;
+    if (has) {
+        const uint32_t local = v - d.vbase;
+        const uint32_t st = d.sbase + local;
+        const float4 a = A[st];
+        const float4 b = B[st];
+        const float nd = __ldg(&D[st].x);
+        sorted[pos] = local;
+        spos[pos] = make_float4(a.x, a.y, a.z, __uint_as_float(local));
+        const f3 fw = forward(xyz(b));
+        sfwd[pos] = make_float4(fw.x, fw.y, fw.z, 0.f);
+        is_due = t_now >= nd;
+    }
+    const uint32_t dm = __ballot_sync(FULL, is_due);
+    if (dm) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&ctl->due_count, (uint32_t)__popc(dm));
+        base = __shfl_sync(FULL, base, 0);
+        if (is_due) due[base + __popc(dm & lanemask_lt())] = make_uint2(pos, (uint32_t)f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                                 StepCtl* __restrict__ ctl,
+                                                 const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
+                                                 const uint32_t* __restrict__ tmp, const float4* __restrict__ A,
+                                                 const float4* __restrict__ B, const float4* __restrict__ D,
+                                                 uint32_t* __restrict__ sorted, float4* __restrict__ spos,
+                                                 float4* __restrict__ sfwd, uint2* __restrict__ due) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
+    for (uint32_t w = gw; w < nocc; w += nw) {
+        const uint32_t b = occ[w];
+        const int f = find_flock_b(fl, nfl, b);
+        const FlockDesc d = fl[f];
+        const float t_now = __fadd_rn(d.time, DT);
+        const uint32_t s0 = __ldg(&offsets[b]), e0 = __ldg(&offsets[b + 1]);
+        if (e0 < s0 || e0 > V) {  // never with a completed scan; skip rather than read out of range
+            if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+            continue;
+        }
+        const uint32_t L = e0 - s0;
+        if (L <= 32) {
+            uint32_t x = lane < L ? tmp[s0 + lane] : 0xFFFFFFFFu;
+            x = bitonic32(x, lane);
+            emit_sorted(lane < L, s0 + lane, x, d, f, t_now, lane, A, B, D, sorted, spos, sfwd, due, ctl);
+        } else {
+            // long range (dense cell or hash collision): rank by counting
+            for (uint32_t c0 = 0; c0 < L; c0 += 32) {
+                const bool has = c0 + lane < L;
+                const uint32_t x = has ? tmp[s0 + c0 + lane] : 0xFFFFFFFFu;
+                uint32_t rank = 0;
+                for (uint32_t j0 = 0; j0 < L; j0 += 32) {
+                    const uint32_t y = (j0 + lane < L) ? tmp[s0 + j0 + lane] : 0xFFFFFFFFu;
+#pragma unroll 8
+                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
+                }
+                emit_sorted(has, s0 + rank, x, d, f, t_now, lane, A, B, D, sorted, spos, sfwd, due, ctl);
+            }
+        }
+    }
+}
+
+
+}  // namespace flk

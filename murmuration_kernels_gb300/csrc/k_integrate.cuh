@@ -1,0 +1,80 @@
+// Pass 6: integrate (reference crates/flock-ref/src/model.rs:149-176;
+// cuda/flock.cu:293-328) and the end-of-step bookkeeping.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace flk {
+
+// ---------------------------------------------------------------------------
+// pass 6: integrate (model.rs:149-176) + end-of-step bookkeeping
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                                   float4* __restrict__ A, float4* __restrict__ B,
+                                                   const float4* __restrict__ C, StepCtl* __restrict__ ctl) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
+        if (!d->remaining) continue;
+        const uint32_t st = d->sbase + (v - d->vbase);
+        const float4 a = A[st];
+        const float4 b = B[st];
+        const float4 c = C[st];
+        f3 vel = xyz(b);
+        const f3 steering = xyz(c);
+        const float roll = a.w;
+
+        const f3 fw = forward(vel);
+        const f3 side = side_of(fw);
+        const float speed = fmaxf(len(vel), 1e-6f);
+        const float a_lat = __fdiv_rn(dot(steering, side), MASS);
+        const float target = clampf(atanf(__fdiv_rn(a_lat, G)), -MAX_BANK, MAX_BANK);
+        const float rate = clampf(__fdiv_rn(__fsub_rn(target, roll), TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
+        const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
+
+        const f3 up = body_up(fw, beta);
+        const float cos_beta = fmaxf(cosf(beta), 0.2f);
+        const float sr = __fdiv_rn(speed, V0);
+        const float sr2 = __fmul_rn(sr, sr);
+        const float lift = __fdiv_rn(__fmul_rn(sr2, L0), cos_beta);
+        const float drag = __fmul_rn(sr2, D0);
+        const f3 flight = sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mul(mul(mk(0.f, 0.f, 1.f), MASS), G));
+        const f3 control = sub(steering, mul(side, dot(steering, side)));
+        vel = add(vel, mul(dvs(add(control, flight), MASS), DT));
+        const float sp = len(vel);
+        if (sp > V_MAX) {
+            vel = mul(vel, __fdiv_rn(V_MAX, sp));
+        } else if (sp < V_MIN && sp > 1e-6f) {
+            vel = mul(vel, __fdiv_rn(V_MIN, sp));
+        }
+        const f3 pos = add(xyz(a), mul(vel, DT));
+        A[st] = make_float4(pos.x, pos.y, pos.z, beta);
+        B[st] = make_float4(vel.x, vel.y, vel.z, rate);
+    }
+    // the last block to finish advances every active flock and resets the step counters
+    __shared__ bool s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&ctl->done_blocks, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int f = threadIdx.x; f < nfl; f += blockDim.x) {
+            if (fl[f].remaining) {
+                fl[f].time = __fadd_rn(fl[f].time, DT);
+                fl[f].remaining -= 1;
+            }
+        }
+        if (threadIdx.x == 0) {
+            ctl->occ_count = 0;
+            ctl->due_count = 0;
+            ctl->scan_ticket = 0;
+            ctl->epoch = ctl->epoch + 1;
+            ctl->done_blocks = 0;
+        }
+    }
+}
+
+
+}  // namespace flk

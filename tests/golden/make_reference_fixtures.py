@@ -180,6 +180,79 @@ def run_reference(drv: Driver, words: np.ndarray, time: float, steps: int):
     return float(t), out, keys1, offs1
 
 
+def time_reference(drv: Driver, n: int, seed: int, steps: int, warmup: int) -> dict:
+    """The reference's own timing protocol (cuda/flock.cu:447-492): per-pass CUDA
+    events around the same launches, mean GPU ms per pass over the timed steps."""
+    from oracle import pyoracle as o
+
+    words = o.scatter(n, seed)
+    B = buckets_for(n)
+    szF = C.sizeof(FlockArg)
+    ks = [drv.fn(m, s) for m, s in (("_Z14grid_histogram5Flock", [szF]), ("_Z16grid_scan_blocks5Flock", [szF]),
+                                     ("_Z16grid_scan_totals5Flockj", [szF, 4]), ("_Z13grid_scan_add5Flock", [szF]),
+                                     ("_Z12grid_scatter5Flock", [szF]), ("_Z6decide5Flockf", [szF, 4]),
+                                     ("_Z9integrate5Flock", [szF]))]
+    f = FlockArg()
+    f.n, f.buckets = n, B
+    for k in ("pos", "vel", "steer"):
+        setattr(f, k, drv.alloc(n * 16))
+    for k in ("roll", "spin", "radius", "next_decision", "centrality", "neighbours", "bucket", "sorted"):
+        setattr(f, k, drv.alloc(n * 4))
+    f.counts = drv.alloc(B * 4)
+    f.offsets = drv.alloc((B + 1) * 4)
+    f.block_sums = drv.alloc((B // SCAN_BLOCK) * 4)
+    w = words
+    f4 = lambda cols: np.concatenate([w[:, cols], np.zeros((n, 1), np.float32)], axis=1)
+    drv.h2d(f.pos, f4([0, 1, 2]))
+    drv.h2d(f.vel, f4([3, 4, 5]))
+    drv.h2d(f.steer, f4([9, 10, 11]))
+    for k, col in (("roll", 6), ("spin", 7), ("radius", 8), ("next_decision", 12), ("neighbours", 13),
+                   ("centrality", 14)):
+        drv.h2d(getattr(f, k), np.ascontiguousarray(w[:, col]))
+    ev = [[C.c_void_p() for _ in range(6)] for _ in range(steps)]
+    for row in ev:
+        for e in row:
+            drv.ck(drv.cu.cuEventCreate(C.byref(e), 0))
+    TB = 256
+    blocks = (n + TB - 1) // TB
+    nblk = C.c_uint32(B // SCAN_BLOCK)
+    t = np.float32(0.0)
+    for s in range(steps):
+        e = ev[s]
+        t = np.float32(t + DT)
+        drv.ck(drv.cu.cuEventRecord(e[0], None))
+        drv.zero(f.counts, B)
+        drv.launch(ks[0], blocks, TB, [f])
+        drv.ck(drv.cu.cuEventRecord(e[1], None))
+        drv.launch(ks[1], B // SCAN_BLOCK, 256, [f])
+        drv.launch(ks[2], 1, 256, [f, nblk])
+        drv.launch(ks[3], (B + TB - 1) // TB, TB, [f])
+        drv.ck(drv.cu.cuEventRecord(e[2], None))
+        drv.launch(ks[4], blocks, TB, [f])
+        drv.ck(drv.cu.cuEventRecord(e[3], None))
+        drv.launch(ks[5], blocks, TB, [f, C.c_float(float(t))])
+        drv.ck(drv.cu.cuEventRecord(e[4], None))
+        drv.launch(ks[6], blocks, TB, [f])
+        drv.ck(drv.cu.cuEventRecord(e[5], None))
+    drv.sync()
+    names = ["grid_histogram", "grid_scan", "grid_scatter", "decide", "integrate"]
+    tot = [0.0] * 5
+    ms = C.c_float()
+    for s in range(warmup, steps):
+        for p in range(5):
+            drv.ck(drv.cu.cuEventElapsedTime_v2(C.byref(ms), ev[s][p], ev[s][p + 1]))
+            tot[p] += ms.value
+    timed = steps - warmup
+    out = {nm: tot[p] / timed for p, nm in enumerate(names)}
+    out["step_total"] = sum(tot) / timed
+    out["bird_steps_per_s"] = n / (out["step_total"] / 1e3)
+    for row in ev:
+        for e in row:
+            drv.cu.cuEventDestroy_v2(e)
+    drv.free()
+    return out
+
+
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
@@ -205,4 +278,12 @@ def main(outdir: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
+    if len(sys.argv) > 1 and sys.argv[1] == "--time":
+        # python tests/golden/make_reference_fixtures.py --time N SEED STEPS WARMUP
+        import json
+
+        n, seed, steps, warmup = (int(x) for x in sys.argv[2:6])
+        print(json.dumps({"birds": n, "seed": seed, "steps": steps, "warmup": warmup,
+                          **time_reference(Driver(), n, seed, steps, warmup)}))
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else HERE)
