@@ -282,6 +282,7 @@ def bench_batched(m, args, local):
         b.add(w)
     b.step(10)  # warm-up (graph capture)
     ms_batched = b.time_steps(K)
+    passes = b.step_timed(5, 0)
     b.close()
     # the same flocks one at a time through the plain step (same graphs, one flock each)
     ms_plain = 0.0
@@ -295,6 +296,7 @@ def bench_batched(m, args, local):
     v_p = total * K / (ms_plain / 1e3)
     return {"value": v_b, "unit": "bird-updates/s", "flocks": 256, "birds": total, "steps": K,
             "ms_per_step": ms_batched / K, "plain_one_at_a_time": v_p, "speedup_vs_plain": v_b / v_p,
+            "passes_ms": {k: round(v, 5) for k, v in passes.items() if k.endswith("_ms")},
             "config": "256 flocks, n log-uniform [1e3, 2e5] (seed 3), flock k seed 3+k, 10-step CUDA graphs"}
 
 

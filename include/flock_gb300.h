@@ -110,6 +110,9 @@ int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t
 int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
 /* Times `steps` graph-launched steps on the batch's stream with CUDA events. */
 int flk_batch_time_steps(flk_batch* b, uint32_t steps, double* ms);
+/* Every flock of the batch, `steps` eager steps with per-pass events; means of
+ * the last steps-warmup steps (as flk_step_timed). */
+int flk_batch_step_timed(flk_batch* b, uint32_t steps, uint32_t warmup, flk_pass_times* out);
 void flk_batch_destroy(flk_batch* b);
 
 /* ---- served: continuous batching of simulate(flock, steps) requests ------ */

@@ -87,6 +87,7 @@ _SIGS = {
     "flk_batch_tune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "flk_batch_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
     "flk_batch_time_steps": (C.c_int, [_P, C.c_uint32, _PD]),
+    "flk_batch_step_timed": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(PassTimes)]),
     "flk_batch_destroy": (None, [_P]),
     "flk_pool_create": (C.c_int, [C.c_int32, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
     "flk_pool_submit": (C.c_int, [_P, C.c_uint32, C.c_float, _PF, C.c_uint32, _PF, _PF, _PU64]),
@@ -354,6 +355,11 @@ class Batch:
         ms = C.c_double()
         _check(lib().flk_batch_time_steps(self._h, steps, C.byref(ms)))
         return ms.value
+
+    def step_timed(self, steps: int, warmup: int = 0) -> dict[str, float]:
+        pt = PassTimes()
+        _check(lib().flk_batch_step_timed(self._h, steps, warmup, C.byref(pt)))
+        return {k: getattr(pt, k) for k, _ in PassTimes._fields_}
 
     def counters(self) -> tuple[int, int, int]:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -360,6 +360,26 @@ extern "C" int flk_batch_time_steps(flk_batch* b, uint32_t steps, double* ms) {
     });
 }
 
+extern "C" int flk_batch_step_timed(flk_batch* b, uint32_t steps, uint32_t warmup, flk_pass_times* out) {
+    if (!b) return fail(FLK_ERR_ARG, "flk_batch_step_timed: null handle");
+    return guarded([&] {
+        std::vector<int> ids = b->eng->flock_ids();
+        b->eng->set_remaining(ids, std::vector<uint32_t>(ids.size(), steps));
+        flk::PassTimes pt{};
+        b->eng->run_timed(steps, warmup, &pt);
+        if (out) {
+            out->hash_ms = pt.ms[0];
+            out->scan_ms = pt.ms[1];
+            out->sort_ms = pt.ms[2];
+            out->decide_ms = pt.ms[3];
+            out->integrate_ms = pt.ms[4];
+            out->total_ms = pt.total_ms;
+            out->timed_steps = pt.timed_steps;
+        }
+        return check_device(*b->eng);
+    });
+}
+
 extern "C" void flk_batch_destroy(flk_batch* b) {
     try {
         delete b;

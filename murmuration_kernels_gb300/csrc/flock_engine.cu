@@ -119,6 +119,12 @@ size_t Engine::bytes_for(uint32_t n) {
 
 void Engine::set_shape(const LaunchShape& s) {
     shape_ = s;
+    // decide's dynamic shared memory grows with its CTA size; allow past 48 KB
+    const int w = s.decide_threads / 32;
+    FLK_CUDA(cudaFuncSetAttribute(k_decide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(w * decide_smem_per_warp<false>())));
+    FLK_CUDA(cudaFuncSetAttribute(k_decide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(w * decide_smem_per_warp<true>())));
     free_graphs();
 }
 
@@ -472,7 +478,9 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
         table_d_, nfl, V_, ctl_, occ_, offsets_, tmp_, A_, B_, D_, sorted_, spos_, sfwd_, due_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
-    const size_t qbytes = (size_t)(shape_.decide_threads / 32) * 64 * 4;  // per-warp hit queues
+    // per-warp hit queue + reduced birds awaiting their epilogue
+    const size_t qbytes = (size_t)(shape_.decide_threads / 32) *
+                          (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, V_, ctl_, due_, offsets_, spos_, sfwd_,
                                                                        B_, C_, D_, radius_table_, sets_);

@@ -17,9 +17,13 @@
 // expensive phase (sqrt, three IEEE divisions, the separation Gaussian,
 // blind-angle test). Only ~11 % of candidates are hits, so this keeps the
 // expensive code on full warps instead of running it for one or two lanes.
+// The cheap phase walks the neighbourhood two 32-candidate chunks at a time so
+// each lane has two loads in flight.
 //
-// Per-lane partial sums are reduced with a fixed shuffle pattern; lane 0
-// finishes the decision in the oracle's order of operations.
+// Per-lane partial sums are reduced with a transposed (reduce-scatter)
+// shuffle pattern straight into shared memory; once 32 birds are reduced, all
+// lanes finish their decisions at once, one bird per lane, in the oracle's
+// order of operations.
 #pragma once
 
 #include "device_common.cuh"
@@ -100,35 +104,90 @@ __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
     }
 }
 
-// Cheap phase over the contiguous candidate range [sc, ec). CHECK_CELL: only
-// birds of cell (cx, cy, cz) count (cell walk, where a bucket can repeat).
+// Queues the lanes' hits; when 32 are waiting, the whole warp takes them.
+template <bool SETS>
+__device__ __forceinline__ void enqueue(Sweep& w, bool hit, uint32_t t, uint32_t lane) {
+    const uint32_t hm = __ballot_sync(FULL, hit);
+    if (!hm) return;
+    if (hit) w.q[w.qn + __popc(hm & lanemask_lt())] = t;
+    w.qn += __popc(hm);
+    if (w.qn >= 32) {
+        __syncwarp();
+        take<SETS>(w, w.q[lane]);
+        const uint32_t extra = w.qn - 32;
+        const uint32_t moved = lane < extra ? w.q[32 + lane] : 0u;
+        __syncwarp();
+        if (lane < extra) w.q[lane] = moved;
+        __syncwarp();
+        w.qn = extra;
+    }
+}
+
+// Cheap-phase test of candidate t; CHECK_CELL also requires cell (cx,cy,cz).
+template <bool CHECK_CELL>
+__device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int cy, int cz) {
+    const float dx = __fsub_rn(q.x, w.p.x), dy = __fsub_rn(q.y, w.p.y), dz = __fsub_rn(q.z, w.p.z);
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    bool hit = d2 <= w.c2;
+    if (CHECK_CELL) hit = hit && cell1(q.x) == cx && cell1(q.y) == cy && cell1(q.z) == cz;
+    return hit;
+}
+
+// Cheap phase over one contiguous candidate range [sc, ec) (wide paths).
 template <bool SETS, bool CHECK_CELL>
 __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32_t lane, int cx = 0, int cy = 0,
                                       int cz = 0) {
     for (uint32_t base = sc; base < ec; base += 32) {
         const uint32_t t = base + lane;
         bool hit = false;
-        if (t < ec && t != w.self) {
-            const float4 q = __ldg(&w.spos[t]);
-            const float dx = __fsub_rn(q.x, w.p.x), dy = __fsub_rn(q.y, w.p.y), dz = __fsub_rn(q.z, w.p.z);
-            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            hit = d2 <= w.c2;
-            if (CHECK_CELL) hit = hit && cell1(q.x) == cx && cell1(q.y) == cy && cell1(q.z) == cz;
+        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.spos[t]), cx, cy, cz);
+        enqueue<SETS>(w, hit, t, lane);
+    }
+}
+
+// Takes the next non-empty bucket range of the neighbourhood (lane c of s/e),
+// warp-uniform; false when none is left.
+__device__ __forceinline__ bool next_range(uint32_t& km, uint32_t s, uint32_t e, uint32_t& b, uint32_t& end) {
+    if (!km) return false;
+    const int c = __ffs(km) - 1;
+    km &= km - 1;
+    b = __shfl_sync(FULL, s, c);
+    end = __shfl_sync(FULL, e, c);
+    return true;
+}
+
+// Cheap phase over the fast path's bucket ranges, two chunks per iteration.
+template <bool SETS>
+__device__ __forceinline__ void sweep_ranges(Sweep& w, uint32_t km, uint32_t s, uint32_t e, uint32_t lane) {
+    uint32_t b0 = 0, e0 = 0;
+    bool have0 = next_range(km, s, e, b0, e0);
+    while (have0) {
+        uint32_t b1 = 0, e1 = 0;
+        bool have1;
+        if (b0 + 32 < e0) {
+            b1 = b0 + 32;
+            e1 = e0;
+            have1 = true;
+        } else {
+            have1 = next_range(km, s, e, b1, e1);
         }
-        const uint32_t hm = __ballot_sync(FULL, hit);
-        if (hm) {
-            if (hit) w.q[w.qn + __popc(hm & lanemask_lt())] = t;
-            w.qn += __popc(hm);
-            if (w.qn >= 32) {
-                __syncwarp();
-                take<SETS>(w, w.q[lane]);
-                const uint32_t extra = w.qn - 32;
-                const uint32_t moved = lane < extra ? w.q[32 + lane] : 0u;
-                __syncwarp();
-                if (lane < extra) w.q[lane] = moved;
-                __syncwarp();
-                w.qn = extra;
-            }
+        const uint32_t tA = b0 + lane, tB = b1 + lane;
+        const bool vA = tA < e0 && tA != w.self;
+        const bool vB = have1 && tB < e1 && tB != w.self;
+        float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
+        if (vA) qA = __ldg(&w.spos[tA]);
+        if (vB) qB = __ldg(&w.spos[tB]);
+        const bool hA = vA && near<false>(w, qA, 0, 0, 0);
+        const bool hB = vB && near<false>(w, qB, 0, 0, 0);
+        enqueue<SETS>(w, hA, tA, lane);
+        enqueue<SETS>(w, hB, tB, lane);
+        if (!have1) break;
+        if (b1 + 32 < e1) {
+            b0 = b1 + 32;
+            e0 = e1;
+            have0 = true;
+        } else {
+            have0 = next_range(km, s, e, b0, e0);
         }
     }
 }
@@ -143,17 +202,40 @@ __device__ __forceinline__ void drain(Sweep& w, uint32_t lane) {
     }
 }
 
-__device__ __forceinline__ float wsum(float x) {
+// Reduce-scatter of K = 2^m values across the warp: afterwards lane l holds the
+// warp total of value index (l >> (5 - m)) & (K - 1) (fixed association).
+template <int K>
+__device__ __forceinline__ float rs_float(float (&v)[K], uint32_t lane) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x = __fadd_rn(x, __shfl_xor_sync(FULL, x, o));
-    return x;
-}
-__device__ __forceinline__ uint32_t wsumu(uint32_t x) {
+    for (int half = K / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool upper = (lane & o) != 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-    return x;
+        for (int i = 0; i < half; ++i) {
+            const float send = upper ? v[i] : v[i + half];
+            const float keep = upper ? v[i + half] : v[i];
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(FULL, send, o));
+        }
+    }
+#pragma unroll
+    for (int o = 16 / K; o >= 1; o >>= 1) v[0] = __fadd_rn(v[0], __shfl_xor_sync(FULL, v[0], o));
+    return v[0];
 }
-__device__ __forceinline__ f3 wsum3(f3 v) { return mk(wsum(v.x), wsum(v.y), wsum(v.z)); }
+template <int K>
+__device__ __forceinline__ uint32_t rs_uint(uint32_t (&v)[K], uint32_t lane) {
+#pragma unroll
+    for (int half = K / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const uint32_t send = upper ? v[i] : v[i + half];
+            const uint32_t keep = upper ? v[i + half] : v[i];
+            v[i] = keep + __shfl_xor_sync(FULL, send, o);
+        }
+    }
+#pragma unroll
+    for (int o = 16 / K; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(FULL, v[0], o);
+    return v[0];
+}
 
 // params.rs:61-65 with the tabulated factor
 __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* __restrict__ rtab) {
@@ -161,31 +243,81 @@ __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* _
     return clampf(__fmul_rn(r, factor), R_H, R_MAX);
 }
 
+// Per-warp shared memory: the hit queue and 32 reduced birds awaiting their epilogue.
+template <bool SETS>
+struct WarpSmem {
+    static constexpr int NI = SETS ? 8 : 4;  // integer sums per bird
+    uint32_t queue[64];
+    float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
+    uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
+    uint32_t st[32];       // arena slot of the bird
+    uint32_t vix[32];      // virtual index (set summaries)
+    float pz[32];          // height (roost pull)
+};
+
+// Finishes bird `slot` of the warp's batch (model.rs:95-144), one lane per bird.
+template <bool SETS>
+__device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot, const float4* __restrict__ Bv,
+                                         float4* __restrict__ C, float4* __restrict__ D,
+                                         const float* __restrict__ rtab, uint32_t* __restrict__ sets) {
+    const uint32_t st = m.st[slot];
+    const f3 sep = mk(m.red[0][slot], m.red[1][slot], m.red[2][slot]);
+    const f3 coh = mk(m.red[3][slot], m.red[4][slot], m.red[5][slot]);
+    const f3 align = mk(m.red[6][slot], m.red[7][slot], m.red[8][slot]);
+    const f3 csum = mk(m.red[9][slot], m.red[10][slot], m.red[11][slot]);
+    const uint32_t n_all = m.cnt[0][slot], n_star = m.cnt[1][slot], n_align = m.cnt[2][slot], n_g = m.cnt[3][slot];
+    const f3 v = xyz(Bv[st]);
+    const float4 cme = C[st];
+    const float nd = D[st].x;
+    const f3 fi = forward(v);
+    f3 force = mk(0.f, 0.f, 0.f);
+    if (n_all > 0) force = add(force, mul(sep, __fdiv_rn(W_SEP, (float)n_all)));
+    const float cen = n_g > 0 ? __fdiv_rn(len(csum), (float)n_g) : 0.0f;
+    if (n_star > 0) force = add(force, mul(normalize_or_zero(coh), __fmul_rn(W_COH, cen)));
+    const f3 al = n_align > 0 ? sub(dvs(align, (float)n_align), fi) : mk(0.f, 0.f, 0.f);
+    force = add(force, mul(al, W_ALIGN));
+    const float roost = __fmul_rn(W_ROOST_V, clampf(__fdiv_rn(__fsub_rn(Z0, m.pz[slot]), H_ROOST_V), -1.0f, 1.0f));
+    force = add(force, mul(mk(0.f, 0.f, 1.f), roost));
+    const float speed = len(v);
+    force = add(force, mul(fi, __fmul_rn(MASS / TAU, __fsub_rn(V0, speed))));
+    C[st] = make_float4(force.x, force.y, force.z, radius_step(cme.w, n_all, rtab));
+    D[st] = make_float4(__fadd_rn(nd, DU), __uint_as_float(n_all), cen, 0.f);
+    if (SETS) {
+        uint32_t* o = sets + (size_t)m.vix[slot] * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = m.cnt[k][slot];
+    }
+}
+
 // CTAs of 256 threads the register budget is sized for (4 -> 64 registers).
 #ifndef FLK_DECIDE_MIN_BLOCKS
 #define FLK_DECIDE_MIN_BLOCKS 4
 #endif
 
-// Shared memory: 64 queue entries (256 B) per warp.
+// Dynamic shared memory: one WarpSmem<SETS> per warp.
 template <bool SETS>
 __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const FlockDesc* __restrict__ fl, uint32_t V,
-                                                   StepCtl* __restrict__ ctl, const uint2* __restrict__ due,
-                                                   const uint32_t* __restrict__ offsets,
-                                                   const float4* __restrict__ spos, const float4* __restrict__ sfwd,
-                                                   const float4* __restrict__ Bv, float4* __restrict__ C,
-                                                   float4* __restrict__ D, const float* __restrict__ rtab,
-                                                   uint32_t* __restrict__ sets) {
-    extern __shared__ uint32_t s_queue[];
+                                                                      StepCtl* __restrict__ ctl,
+                                                                      const uint2* __restrict__ due,
+                                                                      const uint32_t* __restrict__ offsets,
+                                                                      const float4* __restrict__ spos,
+                                                                      const float4* __restrict__ sfwd,
+                                                                      const float4* __restrict__ Bv,
+                                                                      float4* __restrict__ C, float4* __restrict__ D,
+                                                                      const float* __restrict__ rtab,
+                                                                      uint32_t* __restrict__ sets) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    WarpSmem<SETS>& m = reinterpret_cast<WarpSmem<SETS>*>(s_raw)[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t ndue = *(volatile uint32_t*)&ctl->due_count;
-    uint32_t cand = 0, pairs = 0;  // per-warp totals (fit easily in 32 bits)
+    uint32_t cand = 0, pairs = 0, slot = 0;
 
     Sweep w;
     w.spos = spos;
     w.sfwd = sfwd;
-    w.q = s_queue + (threadIdx.x >> 5) * 64;
+    w.q = m.queue;
     w.qn = 0;
 
     for (uint32_t e = gw; e < ndue; e += nw) {
@@ -244,20 +376,14 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
             }
             uint32_t s = 0, en = 0;
             if (keep) bucket_range(offsets, b, V, ctl, s, en);
-            uint32_t km = __ballot_sync(FULL, en > s);
-            while (km) {
-                const int c = __ffs(km) - 1;
-                km &= km - 1;
-                const uint32_t sc = __shfl_sync(FULL, s, c), ec = __shfl_sync(FULL, en, c);
-                cand += ec - sc;
-                sweep<SETS, false>(w, sc, ec, lane);
-            }
+            cand += en - s;
+            sweep_ranges<SETS>(w, __ballot_sync(FULL, en > s), s, en, lane);
         } else {
             uint32_t f0 = __ldg(&offsets[d.bbase]), f1 = __ldg(&offsets[d.bbase + d.buckets]);
             if (f1 < f0 || f1 > V) f1 = f0 = 0;
             if (ncell * 16 >= (long long)(f1 - f0)) {
                 // very wide reach: brute force over the flock's own range
-                cand += f1 - f0;
+                if (lane == 0) cand += f1 - f0;
                 sweep<SETS, false>(w, f0, f1, lane);
             } else {
                 // cell walk with the exact cell check (buckets may repeat)
@@ -281,6 +407,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                             valid = en > s;
                         }
                     }
+                    cand += en - s;
                     uint32_t km = __ballot_sync(FULL, valid);
                     while (km) {
                         const int c = __ffs(km) - 1;
@@ -288,7 +415,6 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                         const uint32_t sc = __shfl_sync(FULL, s, c), ec = __shfl_sync(FULL, en, c);
                         const int ccx = __shfl_sync(FULL, cx, c), ccy = __shfl_sync(FULL, cy, c),
                                   ccz = __shfl_sync(FULL, cz, c);
-                        cand += ec - sc;
                         sweep<SETS, true>(w, sc, ec, lane, ccx, ccy, ccz);
                     }
                 }
@@ -296,45 +422,54 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         }
         drain<SETS>(w, lane);
 
-        // warp reduction (fixed butterfly; lane 0's association is deterministic)
-        const f3 sep = wsum3(w.a.sep), coh = wsum3(w.a.coh), align = wsum3(w.a.align), csum = wsum3(w.a.csum);
-        const uint32_t n_all = wsumu(w.a.n_all), n_star = wsumu(w.a.n_star), n_align = wsumu(w.a.n_align),
-                       n_g = wsumu(w.a.n_g);
-        uint32_t h_all = 0, h_star = 0, h_align = 0, h_g = 0;
+        // reduce-scatter into this bird's slot of the batch
+        {
+            float fv[16] = {w.a.sep.x,  w.a.sep.y,   w.a.sep.z,   w.a.coh.x,  w.a.coh.y,  w.a.coh.z,
+                            w.a.align.x, w.a.align.y, w.a.align.z, w.a.csum.x, w.a.csum.y, w.a.csum.z,
+                            0.f,         0.f,         0.f,         0.f};
+            const float tf = rs_float<16>(fv, lane);
+            if ((lane & 1) == 0) m.red[(lane >> 1) & 15][slot] = tf;
+        }
         if (SETS) {
-            h_all = wsumu(w.a.h_all);
-            h_star = wsumu(w.a.h_star);
-            h_align = wsumu(w.a.h_align);
-            h_g = wsumu(w.a.h_g);
+            uint32_t iv[8] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g,
+                              w.a.h_all, w.a.h_star, w.a.h_align, w.a.h_g};
+            const uint32_t ti = rs_uint<8>(iv, lane);
+            if ((lane & 3) == 0) m.cnt[(lane >> 2) & 7][slot] = ti;
+            if (lane == 12) pairs += ti;  // lane 12 holds n_g
+        } else {
+            uint32_t iv[4] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g};
+            const uint32_t ti = rs_uint<4>(iv, lane);
+            if ((lane & 7) == 0) m.cnt[(lane >> 3) & 3][slot] = ti;
+            if (lane == 24) pairs += ti;  // lane 24 holds n_g
         }
         if (lane == 0) {
-            pairs += n_g;
-            f3 force = mk(0.f, 0.f, 0.f);
-            if (n_all > 0) force = add(force, mul(sep, __fdiv_rn(W_SEP, (float)n_all)));
-            const float cen = n_g > 0 ? __fdiv_rn(len(csum), (float)n_g) : 0.0f;
-            if (n_star > 0) force = add(force, mul(normalize_or_zero(coh), __fmul_rn(W_COH, cen)));
-            const f3 al = n_align > 0 ? sub(dvs(align, (float)n_align), w.fi) : mk(0.f, 0.f, 0.f);
-            force = add(force, mul(al, W_ALIGN));
-            const float roost = __fmul_rn(W_ROOST_V, clampf(__fdiv_rn(__fsub_rn(Z0, p.z), H_ROOST_V), -1.0f, 1.0f));
-            force = add(force, mul(mk(0.f, 0.f, 1.f), roost));
-            const float speed = len(xyz(Bv[st]));  // reloaded: not kept live across the sweep
-            force = add(force, mul(w.fi, __fmul_rn(MASS / TAU, __fsub_rn(V0, speed))));
-            const float nd = D[st].x;
-            C[st] = make_float4(force.x, force.y, force.z, radius_step(C[st].w, n_all, rtab));
-            D[st] = make_float4(__fadd_rn(nd, DU), __uint_as_float(n_all), cen, 0.f);
-            if (SETS) {
-                uint32_t* o = sets + (size_t)(d.vbase + local) * 8;
-                o[0] = n_all; o[1] = n_star; o[2] = n_align; o[3] = n_g;
-                o[4] = h_all; o[5] = h_star; o[6] = h_align; o[7] = h_g;
-            }
+            m.st[slot] = st;
+            m.vix[slot] = d.vbase + local;
+            m.pz[slot] = p.z;
+        }
+        if (++slot == 32) {
+            __syncwarp();
+            epilogue<SETS>(m, lane, Bv, C, D, rtab, sets);
+            __syncwarp();
+            slot = 0;
         }
     }
+    if (slot) {
+        __syncwarp();
+        if (lane < slot) epilogue<SETS>(m, lane, Bv, C, D, rtab, sets);
+    }
     // per-warp totals straight to the counters (no block barrier)
+    const uint32_t cand_w = __reduce_add_sync(FULL, cand), pairs_w = __reduce_add_sync(FULL, pairs);
     if (lane == 0) {
-        if (cand) atomicAdd(&ctl->cand_total, (unsigned long long)cand);
-        if (pairs) atomicAdd(&ctl->pair_total, (unsigned long long)pairs);
+        if (cand_w) atomicAdd(&ctl->cand_total, (unsigned long long)cand_w);
+        if (pairs_w) atomicAdd(&ctl->pair_total, (unsigned long long)pairs_w);
         if (gw == 0) atomicAdd(&ctl->due_total, (unsigned long long)ndue);
     }
+}
+
+template <bool SETS>
+constexpr size_t decide_smem_per_warp() {
+    return sizeof(WarpSmem<SETS>);
 }
 
 }  // namespace flk
