@@ -280,6 +280,9 @@ def bench_batched(m, args, local):
     b = m.Batch(device=local)
     for w in flocks:
         b.add(w)
+    from murmuration_kernels_gb300 import autotune
+
+    tuned = autotune.tune(b, steps=10, use_cache=False)  # launch shapes for this mix
     b.step(10)  # warm-up (graph capture)
     ms_batched = b.time_steps(K)
     passes = b.step_timed(5, 0)
@@ -297,6 +300,7 @@ def bench_batched(m, args, local):
     return {"value": v_b, "unit": "bird-updates/s", "flocks": 256, "birds": total, "steps": K,
             "ms_per_step": ms_batched / K, "plain_one_at_a_time": v_p, "speedup_vs_plain": v_b / v_p,
             "passes_ms": {k: round(v, 5) for k, v in passes.items() if k.endswith("_ms")},
+            "autotuned": {"shape": tuned["shape"], "trials": tuned["trials"]},
             "config": "256 flocks, n log-uniform [1e3, 2e5] (seed 3), flock k seed 3+k, 10-step CUDA graphs"}
 
 
@@ -367,8 +371,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-extra", action="store_true", help="skip the batched / served / CPU measurements")
     ap.add_argument("--batched-steps", type=int, default=30)
-    ap.add_argument("--requests", type=int, default=48)
-    ap.add_argument("--rate", type=float, default=40.0)
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--chunk", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     args = ap.parse_args()

@@ -390,6 +390,12 @@ extern "C" void flk_batch_destroy(flk_batch* b) {
 // ---------------------------------------------------------------------------
 // served: continuous batching
 // ---------------------------------------------------------------------------
+#define FLK_CUDA_ABI(call)                                                               \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) throw Error{FLK_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
 namespace {
 using Clock = std::chrono::steady_clock;
 
@@ -407,91 +413,119 @@ struct Request {
 };
 }  // namespace
 
+struct Retire {
+    std::shared_ptr<Request> r;
+    cudaEvent_t done;  // recorded when the result has reached the caller's buffer
+    float time;
+    bool failed;
+};
+
 struct flk_pool {
     std::unique_ptr<Engine> eng;
     uint64_t budget = 0;
     uint32_t chunk = 10;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_work, cv_done, cv_retire;
     std::deque<uint64_t> queue;                      // tickets waiting for admission, FIFO
     std::map<uint64_t, std::shared_ptr<Request>> reqs;
     std::vector<std::shared_ptr<Request>> resident;  // admitted, in flight
+    std::deque<Retire> retiring;                     // results on their way to the host
     uint64_t next_ticket = 1;
     uint64_t resident_bytes = 0;
-    bool stop = false;
+    bool stop = false, stop_completer = false;
     flk_pool_stats stats{};
-    std::thread worker;
+    std::thread worker, completer;
     std::string worker_error;
 
     void loop();
+    void complete_loop();
+    std::vector<std::shared_ptr<Request>> take_admissions();
 };
 
+// FIFO admission against the memory budget (caller holds no lock).
+std::vector<std::shared_ptr<Request>> flk_pool::take_admissions() {
+    std::vector<std::shared_ptr<Request>> admit;
+    std::lock_guard<std::mutex> lk(mu);
+    while (!queue.empty()) {
+        auto r = reqs.at(queue.front());
+        if (resident_bytes + r->bytes > budget) break;
+        resident_bytes += r->bytes;
+        queue.pop_front();
+        admit.push_back(r);
+    }
+    return admit;
+}
+
+// The device worker. Each turn: admit arrivals (their states start crossing
+// the link on the copy stream while the current chunk runs), wait for the
+// chunk, hand finished flocks' results to the copy stream, launch the next
+// chunk with the new arrivals folded in. Arrivals therefore join at chunk
+// boundaries and their uploads and the results' downloads overlap compute.
 void flk_pool::loop() {
     try {
         cudaSetDevice(eng->device());
+        bool running = false;  // a chunk is in flight on the compute stream
+        auto t0 = Clock::now();
         while (true) {
-            std::vector<std::shared_ptr<Request>> admit;
-            {
+            if (!running) {
                 std::unique_lock<std::mutex> lk(mu);
                 cv_work.wait(lk, [&] { return stop || !queue.empty() || !resident.empty(); });
                 if (stop) return;
-                // admission at a chunk boundary, FIFO, against the memory budget
-                while (!queue.empty()) {
-                    auto r = reqs.at(queue.front());
-                    if (resident_bytes + r->bytes > budget) break;
-                    resident_bytes += r->bytes;
-                    queue.pop_front();
-                    admit.push_back(r);
-                }
+            } else {
+                std::lock_guard<std::mutex> lk(mu);
+                if (stop) return;
             }
-            for (auto& r : admit) {
-                r->flock = eng->add_flock(r->n, r->time, r->words);
+            for (auto& r : take_admissions()) {
+                r->flock = eng->add_flock_async(r->n, r->time, r->words);
                 eng->set_flock_remaining(r->flock, r->steps);
                 std::lock_guard<std::mutex> lk(mu);
                 r->state = 1;
                 resident.push_back(r);
             }
-            std::vector<std::shared_ptr<Request>> live;
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                live = resident;
-            }
-            if (live.empty()) continue;
-            const auto t0 = Clock::now();
-            eng->run(chunk);
-            eng->sync();
-            const uint32_t err = eng->check_device_error();
-            // retire finished flocks: results go straight to the caller's buffers
-            std::vector<std::shared_ptr<Request>> finished;
-            std::vector<int> ids;
-            for (auto& r : live) ids.push_back(r->flock);
-            const std::vector<uint32_t> left = eng->remaining_of(ids);
-            for (size_t k = 0; k < live.size(); ++k)
-                if (left[k] == 0 || err) finished.push_back(live[k]);
-            for (auto& r : finished) {
-                float t = 0.f;
-                if (!err) eng->read_flock(r->flock, &t, r->out_words);
-                eng->remove_flock(r->flock);
-                if (r->out_time) *r->out_time = t;
-            }
-            const auto t1 = Clock::now();
-            {
+            if (running) {
+                eng->sync();
+                running = false;
+                const uint32_t err = eng->check_device_error();
+                std::vector<std::shared_ptr<Request>> live;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    live = resident;
+                }
+                std::vector<int> ids;
+                for (auto& r : live) ids.push_back(r->flock);
+                const std::vector<uint32_t> left = eng->remaining_of(ids);
+                std::vector<Retire> done;
+                for (size_t k = 0; k < live.size(); ++k) {
+                    if (left[k] != 0 && !err) continue;
+                    Retire x{live[k], nullptr, 0.f, err != 0};
+                    FLK_CUDA_ABI(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+                    if (!err) eng->read_flock_async(live[k]->flock, &x.time, live[k]->out_words, x.done);
+                    else FLK_CUDA_ABI(cudaEventRecord(x.done, eng->stream()));
+                    eng->remove_flock(live[k]->flock);
+                    done.push_back(x);
+                }
+                const auto t1 = Clock::now();
                 std::lock_guard<std::mutex> lk(mu);
                 stats.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
                 stats.chunks += 1;
-                for (auto& r : finished) {
-                    r->t_done = t1;
-                    r->state = err ? FLK_ERR_DEVICE : 2;
-                    resident_bytes -= r->bytes;
-                    if (!err) {
-                        stats.completed += 1;
-                        stats.bird_steps += (uint64_t)r->n * r->steps;
-                    }
-                    resident.erase(std::find(resident.begin(), resident.end(), r));
+                for (auto& x : done) {
+                    resident_bytes -= x.r->bytes;  // the slot is reusable in stream order
+                    resident.erase(std::find(resident.begin(), resident.end(), x.r));
+                    retiring.push_back(x);
                 }
                 stats.resident_bytes = resident_bytes;
+                if (!done.empty()) cv_retire.notify_all();
             }
-            if (!finished.empty()) cv_done.notify_all();
+            bool any;
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                any = !resident.empty();
+            }
+            if (any) {
+                t0 = Clock::now();
+                eng->run(chunk);  // launched, not waited for
+                running = true;
+            }
         }
     } catch (const Error& e) {
         std::lock_guard<std::mutex> lk(mu);
@@ -499,6 +533,34 @@ void flk_pool::loop() {
         for (auto& kv : reqs)
             if (kv.second->state == 0 || kv.second->state == 1) kv.second->state = FLK_ERR_CUDA;
         stop = true;
+        cv_done.notify_all();
+    }
+}
+
+// Marks requests done as their results land in the caller's buffers.
+void flk_pool::complete_loop() {
+    cudaSetDevice(eng->device());
+    while (true) {
+        Retire x;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_retire.wait(lk, [&] { return stop_completer || !retiring.empty(); });
+            if (retiring.empty()) return;
+            x = retiring.front();
+        }
+        const cudaError_t e = cudaEventSynchronize(x.done);
+        cudaEventDestroy(x.done);
+        std::lock_guard<std::mutex> lk(mu);
+        retiring.pop_front();
+        x.r->t_done = Clock::now();
+        if (x.r->out_time) *x.r->out_time = x.time;
+        if (x.failed || e != cudaSuccess) {
+            x.r->state = x.failed ? FLK_ERR_DEVICE : FLK_ERR_CUDA;
+        } else {
+            x.r->state = 2;
+            stats.completed += 1;
+            stats.bird_steps += (uint64_t)x.r->n * x.r->steps;
+        }
         cv_done.notify_all();
     }
 }
@@ -516,6 +578,7 @@ extern "C" int flk_pool_create(int32_t device, uint64_t budget_bytes, uint32_t c
         p->eng->set_shape(s);
         flk_pool* raw = p.get();
         p->worker = std::thread([raw] { raw->loop(); });
+        p->completer = std::thread([raw] { raw->complete_loop(); });
         *out = p.release();
         return FLK_OK;
     });
@@ -594,6 +657,13 @@ extern "C" void flk_pool_destroy(flk_pool* p) {
     }
     p->cv_work.notify_all();
     if (p->worker.joinable()) p->worker.join();
+    {
+        // results already on their way still land before the pool goes
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->stop_completer = true;
+    }
+    p->cv_retire.notify_all();
+    if (p->completer.joinable()) p->completer.join();
     try {
         delete p;
     } catch (...) {

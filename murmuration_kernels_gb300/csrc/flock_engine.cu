@@ -78,6 +78,7 @@ Engine::Engine(int device) {
     FLK_CUDA(cudaSetDevice(device_));
     FLK_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
     FLK_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    FLK_CUDA(cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking));
     ctl_ = dalloc<StepCtl>(1, &dev_bytes_);
     StepCtl c{};
     c.epoch = 1;
@@ -95,12 +96,14 @@ Engine::Engine(int device) {
 Engine::~Engine() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    if (copy_) cudaStreamSynchronize(copy_);
     free_graphs();
     dfree(A_); dfree(B_); dfree(C_); dfree(D_);
     dfree(table_d_);
     dfree(key_); dfree(arrival_); dfree(tmp_); dfree(sorted_); dfree(occ_); dfree(due_);
     dfree(spos_); dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
+    if (copy_) cudaStreamDestroy(copy_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -114,7 +117,7 @@ size_t Engine::bytes_for(uint32_t n) {
     // state 64 B + scratch (key, arrival, tmp, sorted, occ 4 B each; due 8 B;
     // spos, sfwd 16 B each) + buckets (counts 4 B + offsets 4 B + status/4096)
     const size_t b = buckets_for(n);
-    return (size_t)n * (64 + 20 + 8 + 32) + b * 8 + (b / SCAN_TILE) * 8 + 256;
+    return (size_t)n * (64 + 20 + 48 + 32) + b * 8 + (b / SCAN_TILE) * 8 + 256;
 }
 
 void Engine::set_shape(const LaunchShape& s) {
@@ -261,6 +264,80 @@ float Engine::flock_time(int id) {
     return slots_[id].time;
 }
 
+int Engine::add_flock_async(uint32_t n, float time, const float* words) {
+    FLK_CUDA(cudaSetDevice(device_));
+    // the state crosses the link on the copy stream while the compute stream
+    // keeps running; a stream-ordered staging buffer is unpacked once it lands
+    float* stage = nullptr;
+    cudaEvent_t landed = nullptr;
+    if (n) {
+        const size_t bytes = (size_t)n * WORDS * 4;
+        FLK_CUDA(cudaMallocAsync((void**)&stage, bytes, copy_));
+        FLK_CUDA(cudaMemcpyAsync(stage, words, bytes, cudaMemcpyHostToDevice, copy_));
+        FLK_CUDA(cudaEventCreateWithFlags(&landed, cudaEventDisableTiming));
+        FLK_CUDA(cudaEventRecord(landed, copy_));
+    }
+    const int id = add_flock(0, time, nullptr);  // reserves the slot; its state follows
+    if (n) {
+        Slot& s = slots_[id];
+        // move the empty reservation to a real range of n birds
+        uint32_t sbase = used_;
+        bool from_hole = false;
+        for (auto& h : free_ranges_) {
+            if (h.second >= n) {
+                sbase = h.first;
+                h.first += n;
+                h.second -= n;
+                from_hole = true;
+                break;
+            }
+        }
+        if (!from_hole) {
+            ensure_arena(used_ + n);
+            used_ += n;
+        }
+        free_ranges_.erase(std::remove_if(free_ranges_.begin(), free_ranges_.end(),
+                                          [](const std::pair<uint32_t, uint32_t>& h) { return h.second == 0; }),
+                           free_ranges_.end());
+        s.n = n;
+        s.sbase = sbase;
+        s.buckets = buckets_for(n);
+        FLK_CUDA(cudaStreamWaitEvent(stream_, landed, 0));
+        const int blocks = std::min<uint32_t>((n + 255) / 256, (uint32_t)num_sms_ * 8);
+        k_unpack<<<blocks, 256, 0, stream_>>>(stage, n, sbase, A_, B_, C_, D_);
+        FLK_CUDA(cudaGetLastError());
+        FLK_CUDA(cudaFreeAsync(stage, stream_));
+        FLK_CUDA(cudaEventDestroy(landed));
+    }
+    return id;
+}
+
+void Engine::read_flock_async(int id, float* time, float* words, cudaEvent_t done) {
+    if (!has_flock(id)) throw Error{-4, "unknown flock id"};
+    FLK_CUDA(cudaSetDevice(device_));
+    sync_times();
+    const Slot& s = slots_[id];
+    if (time) *time = s.time;
+    if (s.n) {
+        // pack on the compute stream (ordered after the steps that wrote the
+        // state), copy out on the copy stream while the next chunk runs
+        const size_t bytes = (size_t)s.n * WORDS * 4;
+        float* stage = nullptr;
+        FLK_CUDA(cudaMallocAsync((void**)&stage, bytes, stream_));
+        const int blocks = std::min<uint32_t>((s.n + 255) / 256, (uint32_t)num_sms_ * 8);
+        k_pack<<<blocks, 256, 0, stream_>>>(stage, s.n, s.sbase, A_, B_, C_, D_);
+        FLK_CUDA(cudaGetLastError());
+        cudaEvent_t packed;
+        FLK_CUDA(cudaEventCreateWithFlags(&packed, cudaEventDisableTiming));
+        FLK_CUDA(cudaEventRecord(packed, stream_));
+        FLK_CUDA(cudaStreamWaitEvent(copy_, packed, 0));
+        FLK_CUDA(cudaMemcpyAsync(words, stage, bytes, cudaMemcpyDeviceToHost, copy_));
+        FLK_CUDA(cudaFreeAsync(stage, copy_));
+        FLK_CUDA(cudaEventDestroy(packed));
+    }
+    FLK_CUDA(cudaEventRecord(done, copy_));
+}
+
 void Engine::read_flock(int id, float* time, float* words) {
     if (!has_flock(id)) throw Error{-4, "unknown flock id"};
     FLK_CUDA(cudaSetDevice(device_));
@@ -294,7 +371,9 @@ void Engine::set_remaining(const std::vector<int>& ids, const std::vector<uint32
 
 void Engine::set_flock_remaining(int id, uint32_t steps) {
     if (!has_flock(id)) throw Error{-4, "unknown flock id"};
-    sync_times();
+    // a flock that is not in the device table has no device-side countdown to
+    // read back, so the host need not wait for work in flight
+    if (std::find(table_ids_.begin(), table_ids_.end(), id) != table_ids_.end()) sync_times();
     slots_[id].remaining = steps;
     table_dirty_ = true;
 }
@@ -428,7 +507,7 @@ void Engine::rebuild_table() {
 void Engine::ensure_scratch() {
     if (V_ > scratch_V_ || !key_) {
         const uint32_t nv = std::max<uint32_t>(V_, scratch_V_ + scratch_V_ / 2);
-        dev_bytes_ -= (size_t)scratch_V_ * (20 + 8 + 32);
+        dev_bytes_ -= (size_t)scratch_V_ * (20 + 48 + 32);
         dfree(key_); dfree(arrival_); dfree(tmp_); dfree(sorted_); dfree(occ_); dfree(due_);
         dfree(spos_); dfree(sfwd_); dfree(sets_);
         key_ = dalloc<uint32_t>(nv, &dev_bytes_);
@@ -436,7 +515,7 @@ void Engine::ensure_scratch() {
         tmp_ = dalloc<uint32_t>(nv, &dev_bytes_);
         sorted_ = dalloc<uint32_t>(nv, &dev_bytes_);
         occ_ = dalloc<uint32_t>(nv, &dev_bytes_);
-        due_ = dalloc<uint2>(nv, &dev_bytes_);
+        due_ = dalloc<DueRec>(nv, &dev_bytes_);
         spos_ = dalloc<float4>(nv, &dev_bytes_);
         sfwd_ = dalloc<float4>(nv, &dev_bytes_);
         scratch_V_ = nv;
@@ -475,17 +554,17 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
     k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
-        table_d_, nfl, V_, ctl_, occ_, offsets_, tmp_, A_, B_, D_, sorted_, spos_, sfwd_, due_);
+        table_d_, nfl, V_, ctl_, occ_, offsets_, tmp_, A_, B_, C_, D_, sorted_, spos_, sfwd_, due_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
     // per-warp hit queue + reduced birds awaiting their epilogue
     const size_t qbytes = (size_t)(shape_.decide_threads / 32) *
                           (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
-        k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, V_, ctl_, due_, offsets_, spos_, sfwd_,
+        k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(V_, ctl_, due_, offsets_, spos_, sfwd_,
                                                                        B_, C_, D_, radius_table_, sets_);
     else
-        k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, V_, ctl_, due_, offsets_, spos_,
+        k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(V_, ctl_, due_, offsets_, spos_,
                                                                         sfwd_, B_, C_, D_, radius_table_, nullptr);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
     k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, B_, C_, ctl_);

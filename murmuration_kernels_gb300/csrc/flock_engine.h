@@ -42,6 +42,14 @@ struct StepCtl {
     unsigned long long pad2;
 };
 
+// One deciding bird, written by the per-bucket sort so that decide can start
+// from a single record (48 B, three 16-byte loads from one place).
+struct __align__(16) DueRec {
+    float4 pr;  // position xyz, radius
+    float4 fk;  // unit heading xyz, index in the cell-ordered view (u32 bits)
+    uint4 fl;   // arena slot, bucket base, bucket count, virtual index
+};
+
 enum DeviceError : uint32_t {
     DEV_OK = 0,
     DEV_SCAN_TIMEOUT = 1,  // a scan look-back wait gave up
@@ -78,6 +86,13 @@ public:
 
     // Flocks. `words` is a host array of n*15 .flk words (any host memory).
     int add_flock(uint32_t n, float time, const float* words);  // returns id >= 0
+    // Same, but the host-to-device copy runs on the copy stream and overlaps
+    // the compute stream's work; `words` must stay valid until the next sync.
+    int add_flock_async(uint32_t n, float time, const float* words);
+    // Packs the flock on the compute stream and copies it out on the copy
+    // stream; `done` (an event) is recorded when `words` holds the result.
+    // The slot may be removed right after the call (stream order protects it).
+    void read_flock_async(int id, float* time, float* words, cudaEvent_t done);
     void remove_flock(int id);
     void read_flock(int id, float* time, float* words);  // D2H + pack
     float flock_time(int id);
@@ -135,6 +150,7 @@ private:
 
     int device_ = 0, num_sms_ = 0;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t copy_ = nullptr;  // host<->device state copies of the serving pool
     LaunchShape shape_;
     size_t dev_bytes_ = 0;
 
@@ -156,7 +172,7 @@ private:
     // scratch (virtual / sorted order)
     uint32_t scratch_V_ = 0, scratch_B_ = 0;
     uint32_t *key_ = nullptr, *arrival_ = nullptr, *tmp_ = nullptr, *sorted_ = nullptr, *occ_ = nullptr;
-    uint2* due_ = nullptr;
+    DueRec* due_ = nullptr;
     float4 *spos_ = nullptr, *sfwd_ = nullptr;  // cell-ordered view read by decide
     uint32_t *counts_ = nullptr, *offsets_ = nullptr;
     unsigned long long* status_ = nullptr;

@@ -296,9 +296,8 @@ __device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot,
 
 // Dynamic shared memory: one WarpSmem<SETS> per warp.
 template <bool SETS>
-__global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const FlockDesc* __restrict__ fl, uint32_t V,
-                                                                      StepCtl* __restrict__ ctl,
-                                                                      const uint2* __restrict__ due,
+__global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(uint32_t V, StepCtl* __restrict__ ctl,
+                                                                      const DueRec* __restrict__ due,
                                                                       const uint32_t* __restrict__ offsets,
                                                                       const float4* __restrict__ spos,
                                                                       const float4* __restrict__ sfwd,
@@ -321,15 +320,12 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
     w.qn = 0;
 
     for (uint32_t e = gw; e < ndue; e += nw) {
-        const uint2 ent = due[e];
-        const uint32_t k = ent.x;
-        const FlockDesc d = fl[ent.y];
-        const float4 me = spos[k];
-        const uint32_t local = __float_as_uint(me.w);
-        const uint32_t st = d.sbase + local;
-        const float r = C[st].w;
-        w.p = mk(me.x, me.y, me.z);
-        w.fi = forward(xyz(Bv[st]));
+        const DueRec rec = due[e];  // everything the setup needs, one place
+        const uint32_t k = __float_as_uint(rec.fk.w);
+        const uint32_t st = rec.fl.x, bbase = rec.fl.y, buckets = rec.fl.z;
+        const float r = rec.pr.w;
+        w.p = mk(rec.pr.x, rec.pr.y, rec.pr.z);
+        w.fi = mk(rec.fk.x, rec.fk.y, rec.fk.z);
         w.r2 = __fmul_rn(r, r);
         const float rr = __fmul_rn(2.0f, r);
         w.c2 = __fmul_rn(rr, rr);
@@ -347,7 +343,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         const bool wide = nxl > (1 << 20) || nyl > (1 << 20) || nzl > (1 << 20);
         const long long ncell = wide ? (1ll << 62) : nxl * nyl * nzl;
         const int nx = (int)nxl, ny = (int)nyl;
-        const uint32_t mask = d.buckets - 1u;
+        const uint32_t mask = buckets - 1u;
 
         w.a.sep = w.a.coh = w.a.align = w.a.csum = mk(0.f, 0.f, 0.f);
         w.a.n_all = w.a.n_star = w.a.n_align = w.a.n_g = 0;
@@ -366,7 +362,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                 const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
                 const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                 valid = dx * dx + dy * dy + dz * dz <= reach2;
-                b = d.bbase + (cell_hash(cx, cy, cz) & mask);
+                b = bbase + (cell_hash(cx, cy, cz) & mask);
             }
             const uint32_t vm = __ballot_sync(FULL, valid);
             bool keep = false;
@@ -379,7 +375,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
             cand += en - s;
             sweep_ranges<SETS>(w, __ballot_sync(FULL, en > s), s, en, lane);
         } else {
-            uint32_t f0 = __ldg(&offsets[d.bbase]), f1 = __ldg(&offsets[d.bbase + d.buckets]);
+            uint32_t f0 = __ldg(&offsets[bbase]), f1 = __ldg(&offsets[bbase + buckets]);
             if (f1 < f0 || f1 > V) f1 = f0 = 0;
             if (ncell * 16 >= (long long)(f1 - f0)) {
                 // very wide reach: brute force over the flock's own range
@@ -403,7 +399,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                         const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                         valid = dx * dx + dy * dy + dz * dz <= reach2;
                         if (valid) {
-                            bucket_range(offsets, d.bbase + (cell_hash(cx, cy, cz) & mask), V, ctl, s, en);
+                            bucket_range(offsets, bbase + (cell_hash(cx, cy, cz) & mask), V, ctl, s, en);
                             valid = en > s;
                         }
                     }
@@ -444,7 +440,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         }
         if (lane == 0) {
             m.st[slot] = st;
-            m.vix[slot] = d.vbase + local;
+            m.vix[slot] = rec.fl.w;
             m.pz[slot] = p.z;
         }
         if (++slot == 32) {

@@ -220,21 +220,27 @@ __device__ __forceinline__ uint32_t bitonic32(uint32_t x, uint32_t lane) {
     return x;
 }
 
-__device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, const FlockDesc& d, int f, float t_now,
+// Writes one bird of the cell-ordered view at sorted slot `pos` and, when it
+// decides this step, its self-contained decide record. Called by all 32 lanes.
+__device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, const FlockDesc& d, float t_now,
                                             uint32_t lane, const float4* __restrict__ A, const float4* __restrict__ B,
-                                            const float4* __restrict__ D, uint32_t* __restrict__ sorted,
-                                            float4* __restrict__ spos, float4* __restrict__ sfwd,
-                                            uint2* __restrict__ due, StepCtl* __restrict__ ctl) {
+                                            const float4* __restrict__ C, const float4* __restrict__ D,
+                                            uint32_t* __restrict__ sorted, float4* __restrict__ spos,
+                                            float4* __restrict__ sfwd, DueRec* __restrict__ due,
+                                            StepCtl* __restrict__ ctl) {
     bool is_due = false;
+    uint32_t local = 0, st = 0;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    f3 fw = mk(0.f, 0.f, 0.f);
     if (has) {
-        const uint32_t local = v - d.vbase;
-        const uint32_t st = d.sbase + local;
-        const float4 a = A[st];
+        local = v - d.vbase;
+        st = d.sbase + local;
+        a = A[st];
         const float4 b = B[st];
         const float nd = __ldg(&D[st].x);
         sorted[pos] = local;
         spos[pos] = make_float4(a.x, a.y, a.z, __uint_as_float(local));
-        const f3 fw = forward(xyz(b));
+        fw = forward(xyz(b));
         sfwd[pos] = make_float4(fw.x, fw.y, fw.z, 0.f);
         is_due = t_now >= nd;
     }
@@ -243,7 +249,13 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, 
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&ctl->due_count, (uint32_t)__popc(dm));
         base = __shfl_sync(FULL, base, 0);
-        if (is_due) due[base + __popc(dm & lanemask_lt())] = make_uint2(pos, (uint32_t)f);
+        if (is_due) {
+            DueRec r;
+            r.pr = make_float4(a.x, a.y, a.z, __ldg(&C[st].w));
+            r.fk = make_float4(fw.x, fw.y, fw.z, __uint_as_float(pos));
+            r.fl = make_uint4(st, d.bbase, d.buckets, d.vbase + local);
+            due[base + __popc(dm & lanemask_lt())] = r;
+        }
     }
 }
 
@@ -251,9 +263,10 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
                                                  const uint32_t* __restrict__ tmp, const float4* __restrict__ A,
-                                                 const float4* __restrict__ B, const float4* __restrict__ D,
-                                                 uint32_t* __restrict__ sorted, float4* __restrict__ spos,
-                                                 float4* __restrict__ sfwd, uint2* __restrict__ due) {
+                                                 const float4* __restrict__ B, const float4* __restrict__ C,
+                                                 const float4* __restrict__ D, uint32_t* __restrict__ sorted,
+                                                 float4* __restrict__ spos, float4* __restrict__ sfwd,
+                                                 DueRec* __restrict__ due) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -272,7 +285,7 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
         if (L <= 32) {
             uint32_t x = lane < L ? tmp[s0 + lane] : 0xFFFFFFFFu;
             x = bitonic32(x, lane);
-            emit_sorted(lane < L, s0 + lane, x, d, f, t_now, lane, A, B, D, sorted, spos, sfwd, due, ctl);
+            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, A, B, C, D, sorted, spos, sfwd, due, ctl);
         } else {
             // long range (dense cell or hash collision): rank by counting
             for (uint32_t c0 = 0; c0 < L; c0 += 32) {
@@ -284,7 +297,7 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
 #pragma unroll 8
                     for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
                 }
-                emit_sorted(has, s0 + rank, x, d, f, t_now, lane, A, B, D, sorted, spos, sfwd, due, ctl);
+                emit_sorted(has, s0 + rank, x, d, t_now, lane, A, B, C, D, sorted, spos, sfwd, due, ctl);
             }
         }
     }
