@@ -550,24 +550,33 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
     if (ev) FLK_CUDA(cudaEventRecord(ev[0], stream_));
     k_hash_count<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, key_, arrival_, counts_, occ_, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
-    k_scan<<<ntiles, SCAN_THREADS, 0, stream_>>>(counts_, offsets_, ntiles, status_, ctl_);
+    if (sets) {
+        // a step that reports its grid builds the canonical dense offsets
+        // (every bucket, in bucket order) and uses them as the run starts
+        k_scan<<<ntiles, SCAN_THREADS, 0, stream_>>>(counts_, offsets_, ntiles, status_, ctl_);
+    } else {
+        k_alloc<<<pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256), 256, 0, stream_>>>(table_d_, nfl, occ_,
+                                                                                           counts_, offsets_, ctl_);
+    }
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
     k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
-        table_d_, nfl, V_, ctl_, occ_, offsets_, tmp_, A_, B_, C_, D_, sorted_, spos_, sfwd_, due_);
+        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, A_, B_, C_, D_, sorted_, spos_, sfwd_, due_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
     // per-warp hit queue + reduced birds awaiting their epilogue
     const size_t qbytes = (size_t)(shape_.decide_threads / 32) *
                           (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
-        k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(V_, ctl_, due_, offsets_, spos_, sfwd_,
-                                                                       B_, C_, D_, radius_table_, sets_);
+        k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
+                                                                       counts_, spos_, sfwd_, B_, C_, D_,
+                                                                       radius_table_, sets_);
     else
-        k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(V_, ctl_, due_, offsets_, spos_,
-                                                                        sfwd_, B_, C_, D_, radius_table_, nullptr);
+        k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
+                                                                        counts_, spos_, sfwd_, B_, C_, D_,
+                                                                        radius_table_, nullptr);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
-    k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, B_, C_, ctl_);
+    k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, B_, C_, counts_, occ_, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
 }
 

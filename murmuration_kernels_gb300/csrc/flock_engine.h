@@ -22,7 +22,7 @@ struct FlockDesc {
     uint32_t buckets;    // power of two, buckets_for(n)
     uint32_t remaining;  // steps still to run; 0 = idle this step
     float time;          // world clock (f32, as the reference keeps it)
-    uint32_t pad;
+    uint32_t cursor;     // next free slot of the flock's view region (bucket allocation; reset per step)
 };
 
 // Step-control block in device memory: per-step counters (reset by the last

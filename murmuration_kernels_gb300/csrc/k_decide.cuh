@@ -46,13 +46,18 @@ __device__ __forceinline__ uint32_t set_mix(uint32_t j) {
     return h;
 }
 
-// Bucket range [s, e) of bucket b; an inconsistent range (only possible if the
-// scan gave up) is recorded and treated as empty instead of being read.
-__device__ __forceinline__ void bucket_range(const uint32_t* __restrict__ offsets, uint32_t b, uint32_t V,
+// Bucket range [s, e) of bucket b: its start (offsets) and length (counts). An
+// empty bucket's start is stale and never used; an inconsistent range (only
+// possible if the grid build gave up) is recorded and treated as empty.
+__device__ __forceinline__ void bucket_range(const uint32_t* __restrict__ offsets,
+                                             const uint32_t* __restrict__ counts, uint32_t b, uint32_t V,
                                              StepCtl* __restrict__ ctl, uint32_t& s, uint32_t& e) {
+    const uint32_t c = __ldg(&counts[b]);
     s = __ldg(&offsets[b]);
-    e = __ldg(&offsets[b + 1]);
-    if (e < s || e > V) {
+    e = s + c;
+    if (c == 0) {
+        e = s = 0;
+    } else if (e < s || e > V) {
         atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
         e = s = 0;
     }
@@ -296,9 +301,11 @@ __device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot,
 
 // Dynamic shared memory: one WarpSmem<SETS> per warp.
 template <bool SETS>
-__global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(uint32_t V, StepCtl* __restrict__ ctl,
+__global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const FlockDesc* __restrict__ fl, int nfl,
+                                                                      uint32_t V, StepCtl* __restrict__ ctl,
                                                                       const DueRec* __restrict__ due,
                                                                       const uint32_t* __restrict__ offsets,
+                                                                      const uint32_t* __restrict__ counts,
                                                                       const float4* __restrict__ spos,
                                                                       const float4* __restrict__ sfwd,
                                                                       const float4* __restrict__ Bv,
@@ -371,11 +378,13 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(uint32_t 
                 keep = (int)lane == __ffs(peers) - 1;
             }
             uint32_t s = 0, en = 0;
-            if (keep) bucket_range(offsets, b, V, ctl, s, en);
+            if (keep) bucket_range(offsets, counts, b, V, ctl, s, en);
             cand += en - s;
             sweep_ranges<SETS>(w, __ballot_sync(FULL, en > s), s, en, lane);
         } else {
-            uint32_t f0 = __ldg(&offsets[bbase]), f1 = __ldg(&offsets[bbase + buckets]);
+            // the flock's own view region [vbase, vbase + n)
+            const FlockDesc* fd = &fl[find_flock_v(fl, nfl, rec.fl.w)];
+            uint32_t f0 = __ldg(&fd->vbase), f1 = f0 + __ldg(&fd->n);
             if (f1 < f0 || f1 > V) f1 = f0 = 0;
             if (ncell * 16 >= (long long)(f1 - f0)) {
                 // very wide reach: brute force over the flock's own range
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(uint32_t 
                         const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                         valid = dx * dx + dy * dy + dz * dz <= reach2;
                         if (valid) {
-                            bucket_range(offsets, bbase + (cell_hash(cx, cy, cz) & mask), V, ctl, s, en);
+                            bucket_range(offsets, counts, bbase + (cell_hash(cx, cy, cz) & mask), V, ctl, s, en);
                             valid = en > s;
                         }
                     }

@@ -88,7 +88,7 @@ __device__ __forceinline__ unsigned long long scan_word(uint32_t epoch, uint32_t
     return ((unsigned long long)(epoch & 0x3FFFFFFFu) << 34) | ((unsigned long long)flag << 32) | value;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
                                                        uint32_t ntiles, unsigned long long* __restrict__ status,
                                                        StepCtl* __restrict__ ctl) {
     __shared__ uint32_t s_tile, s_prefix;
@@ -105,11 +105,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(uint32_t* __restrict__ co
     const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
 
     uint4 c[SCAN_ITEMS / 4];
-    uint4* src = reinterpret_cast<uint4*>(counts + base);
+    const uint4* src = reinterpret_cast<const uint4*>(counts + base);
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS / 4; ++k) c[k] = src[k];
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS / 4; ++k) src[k] = make_uint4(0, 0, 0, 0);  // histogram ready for next step
     uint32_t sum = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS / 4; ++k) sum += c[k].x + c[k].y + c[k].z + c[k].w;
@@ -188,6 +186,52 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(uint32_t* __restrict__ co
 }
 
 // ---------------------------------------------------------------------------
+// pass 2' (steps without grid output): place each occupied bucket's run
+// ---------------------------------------------------------------------------
+// Production steps need each occupied bucket's birds contiguous, not the dense
+// canonical offsets, so instead of scanning every bucket this pass gives each
+// occupied bucket a start inside its flock's view region [vbase, vbase + n)
+// from a per-flock cursor: one atomicAdd per warp when the warp's buckets
+// share a flock (the usual case), one per bucket otherwise. Where a run lands
+// does not change any result: decide visits buckets in cell order and each
+// run in bird order. The start is written to offsets[b]; the bucket's length
+// stays in counts[b] until integrate clears it.
+__global__ void __launch_bounds__(256) k_alloc(FlockDesc* __restrict__ fl, int nfl, const uint32_t* __restrict__ occ,
+                                               const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
+                                               StepCtl* __restrict__ ctl) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nocc; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + lane;
+        const bool act = i < nocc;
+        uint32_t b = 0, c = 0;
+        int f = -1;
+        if (act) {
+            b = occ[i];
+            c = counts[b];
+            f = find_flock_b(fl, nfl, b);
+        }
+        const uint32_t am = __ballot_sync(FULL, act);
+        const int f0 = __shfl_sync(FULL, f, __ffs(am) - 1);
+        if (__all_sync(FULL, !act || f == f0)) {
+            // one flock: warp prefix of the run lengths + one atomic
+            uint32_t inc = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, inc, o);
+                if ((int)lane >= o) inc += y;
+            }
+            uint32_t base = 0;
+            if (lane == 31) base = atomicAdd(&fl[f0].cursor, inc);
+            base = __shfl_sync(FULL, base, 31) + __ldg(&fl[f0].vbase);
+            if (act) offsets[b] = base + inc - c;
+        } else if (act) {
+            offsets[b] = __ldg(&fl[f].vbase) + atomicAdd(&fl[f].cursor, c);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // pass 3: scatter by arrival rank
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
@@ -262,6 +306,7 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, 
 __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
+                                                 const uint32_t* __restrict__ counts,
                                                  const uint32_t* __restrict__ tmp, const float4* __restrict__ A,
                                                  const float4* __restrict__ B, const float4* __restrict__ C,
                                                  const float4* __restrict__ D, uint32_t* __restrict__ sorted,
@@ -276,12 +321,11 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
         const int f = find_flock_b(fl, nfl, b);
         const FlockDesc d = fl[f];
         const float t_now = __fadd_rn(d.time, DT);
-        const uint32_t s0 = __ldg(&offsets[b]), e0 = __ldg(&offsets[b + 1]);
-        if (e0 < s0 || e0 > V) {  // never with a completed scan; skip rather than read out of range
+        const uint32_t s0 = __ldg(&offsets[b]), L = __ldg(&counts[b]);
+        if (s0 + L > V || s0 + L < s0) {  // never with valid starts; skip rather than read out of range
             if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
             continue;
         }
-        const uint32_t L = e0 - s0;
         if (L <= 32) {
             uint32_t x = lane < L ? tmp[s0 + lane] : 0xFFFFFFFFu;
             x = bitonic32(x, lane);

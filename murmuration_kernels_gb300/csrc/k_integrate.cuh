@@ -11,7 +11,11 @@ namespace flk {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                    float4* __restrict__ A, float4* __restrict__ B,
-                                                   const float4* __restrict__ C, StepCtl* __restrict__ ctl) {
+                                                   const float4* __restrict__ C, uint32_t* __restrict__ counts,
+                                                   const uint32_t* __restrict__ occ, StepCtl* __restrict__ ctl) {
+    // the histogram's occupied entries go back to zero for the next step
+    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nocc; i += gridDim.x * blockDim.x) counts[occ[i]] = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
         if (!d->remaining) continue;
@@ -61,6 +65,7 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
     if (s_last) {
         __threadfence();
         for (int f = threadIdx.x; f < nfl; f += blockDim.x) {
+            fl[f].cursor = 0;
             if (fl[f].remaining) {
                 fl[f].time = __fadd_rn(fl[f].time, DT);
                 fl[f].remaining -= 1;
