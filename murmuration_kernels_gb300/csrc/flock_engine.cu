@@ -116,7 +116,7 @@ void Engine::free_graphs() {
 size_t Engine::bytes_for(uint32_t n) {
     // state 64 B + scratch (key, arrival, tmp, sorted, occ 4 B each; due 8 B;
     // spos, sfwd 16 B each) + buckets (counts 4 B + offsets 4 B + status/4096)
-    const size_t b = buckets_for(n);
+    const size_t b = production_buckets(n);
     return (size_t)n * (64 + 20 + 48 + 32) + b * 8 + (b / SCAN_TILE) * 8 + 256;
 }
 
@@ -396,10 +396,7 @@ std::vector<uint32_t> Engine::remaining_of(const std::vector<int>& ids) {
 
 double Engine::time_run(uint32_t steps) {
     FLK_CUDA(cudaSetDevice(device_));
-    if (table_dirty_) {
-        sync_times();
-        rebuild_table();
-    }
+    prepare(false);
     cudaEvent_t e0, e1;
     FLK_CUDA(cudaEventCreate(&e0));
     FLK_CUDA(cudaEventCreate(&e1));
@@ -423,10 +420,7 @@ __global__ void k_flush(uint4* __restrict__ buf, size_t n16, uint32_t salt) {
 
 void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_step) {
     FLK_CUDA(cudaSetDevice(device_));
-    if (table_dirty_) {
-        sync_times();
-        rebuild_table();
-    }
+    prepare(false);
     if (table_h_.empty() || steps == 0) return;
     uint4* flush = nullptr;
     const size_t n16 = flush_bytes / 16;
@@ -462,7 +456,24 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     table_dirty_ = true;
 }
 
-void Engine::rebuild_table() {
+// Bucket count of a production step: the canonical rule without its 2^22
+// clamp, so flocks above 2M birds keep hash collisions as rare as smaller
+// ones (a production step reports no keys; any count gives the same sets).
+uint32_t production_buckets(uint32_t n) {
+    uint64_t want = 1;
+    while (want < (uint64_t)n * 2) want <<= 1;
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 1u << 16), 1u << 27);
+}
+
+void Engine::prepare(bool grid_output) {
+    if (table_dirty_ || table_grid_output_ != grid_output) {
+        sync_times();
+        rebuild_table(grid_output);
+    }
+}
+
+void Engine::rebuild_table(bool grid_output) {
+    table_grid_output_ = grid_output;
     std::vector<FlockDesc> t;
     std::vector<int> ids;
     uint32_t V = 0;
@@ -475,13 +486,13 @@ void Engine::rebuild_table() {
         d.n = s.n;
         d.sbase = s.sbase;
         d.bbase = (uint32_t)Bt;
-        d.buckets = s.buckets;
+        d.buckets = grid_output ? s.buckets : production_buckets(s.n);
         d.remaining = s.remaining;
         d.time = s.time;
         t.push_back(d);
         ids.push_back((int)k);
         V += s.n;
-        Bt += s.buckets;
+        Bt += d.buckets;
     }
     if (Bt >= (1ull << 32) - SCAN_TILE) throw Error{-5, "too many buckets in one batch"};
     if ((uint32_t)t.size() > table_cap_ || !table_d_) {
@@ -596,10 +607,7 @@ void Engine::ensure_graph() {
 
 void Engine::run(uint32_t steps) {
     FLK_CUDA(cudaSetDevice(device_));
-    if (table_dirty_) {
-        sync_times();
-        rebuild_table();
-    }
+    prepare(false);
     if (table_h_.empty() || steps == 0) return;
     const uint32_t chunk = (uint32_t)std::max(1, shape_.graph_chunk);
     uint32_t done = 0;
@@ -625,10 +633,7 @@ void Engine::run(uint32_t steps) {
 
 void Engine::run_timed(uint32_t steps, uint32_t warmup, PassTimes* out) {
     FLK_CUDA(cudaSetDevice(device_));
-    if (table_dirty_) {
-        sync_times();
-        rebuild_table();
-    }
+    prepare(false);
     PassTimes pt{};
     if (table_h_.empty() || steps == 0) {
         if (out) *out = pt;
@@ -663,10 +668,7 @@ void Engine::run_timed(uint32_t steps, uint32_t warmup, PassTimes* out) {
 
 void Engine::step_debug(std::vector<GridDebug>* out) {
     FLK_CUDA(cudaSetDevice(device_));
-    if (table_dirty_) {
-        sync_times();
-        rebuild_table();
-    }
+    prepare(true);  // the canonical bucket counts the reported grid is defined with
     if (table_h_.empty()) return;
     if (!sets_) sets_ = dalloc<uint32_t>((size_t)scratch_V_ * 8, &dev_bytes_);
     FLK_CUDA(cudaMemsetAsync(sets_, 0, (size_t)V_ * 8 * 4, stream_));

@@ -141,7 +141,8 @@ private:
         bool live = false;
     };
     void ensure_arena(uint32_t need);
-    void rebuild_table();
+    void rebuild_table(bool grid_output);
+    void prepare(bool grid_output);  // rebuild the table if stale or built for the other mode
     void ensure_scratch();
     void enqueue_step(bool sets, cudaEvent_t* ev = nullptr);
     void free_graphs();
@@ -162,6 +163,7 @@ private:
 
     // flock table of flocks with remaining > 0, in slot order
     bool table_dirty_ = true;
+    bool table_grid_output_ = false;  // table built with canonical bucket counts (grid-reporting step)
     bool device_ahead_ = false;  // steps ran since the host last read the device table
     std::vector<FlockDesc> table_h_;
     std::vector<int> table_ids_;
@@ -188,6 +190,8 @@ private:
 
 // Canonical bucket count for a flock of n birds (reference cuda/flock.cu:368-372).
 uint32_t buckets_for(uint32_t n);
+// Bucket count of a production step (the same rule without the 2^22 clamp).
+uint32_t production_buckets(uint32_t n);
 
 // Device-error and CUDA failures surface as this exception inside the library;
 // the C ABI turns it into a status code and a message.

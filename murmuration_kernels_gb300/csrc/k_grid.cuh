@@ -264,6 +264,41 @@ __device__ __forceinline__ uint32_t bitonic32(uint32_t x, uint32_t lane) {
     return x;
 }
 
+// Bitonic sort of 32*R keys held R per lane (element i = lane + 32*k in x[k]),
+// ascending; stages with stride >= 32 swap between a lane's own registers.
+template <int R>
+__device__ __forceinline__ void bitonic_lanes(uint32_t (&x)[R], uint32_t lane) {
+    constexpr int N = 32 * R;
+#pragma unroll
+    for (int s = 2; s <= N; s <<= 1) {
+#pragma unroll
+        for (int j = s >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    const int kp = k ^ jr;
+                    if (kp > k) {  // x[k] is the lower element of the pair
+                        const bool up = ((lane + 32u * k) & (uint32_t)s) == 0;
+                        const uint32_t a = x[k], b = x[kp];
+                        x[k] = up ? min(a, b) : max(a, b);
+                        x[kp] = up ? max(a, b) : min(a, b);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    const uint32_t i = lane + 32u * k;
+                    const uint32_t y = __shfl_xor_sync(FULL, x[k], j);
+                    const bool up = (i & (uint32_t)s) == 0;
+                    const bool lower = (i & (uint32_t)j) == 0;
+                    x[k] = (lower == up) ? min(x[k], y) : max(x[k], y);
+                }
+            }
+        }
+    }
+}
+
 // Writes one bird of the cell-ordered view at sorted slot `pos` and, when it
 // decides this step, its self-contained decide record. Called by all 32 lanes.
 __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, const FlockDesc& d, float t_now,
@@ -330,6 +365,24 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             uint32_t x = lane < L ? tmp[s0 + lane] : 0xFFFFFFFFu;
             x = bitonic32(x, lane);
             emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, A, B, C, D, sorted, spos, sfwd, due, ctl);
+        } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
+            uint32_t x[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : 0xFFFFFFFFu;
+            bitonic_lanes<2>(x, lane);
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, A, B, C, D, sorted, spos,
+                            sfwd, due, ctl);
+        } else if (L <= 128) {
+            uint32_t x[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : 0xFFFFFFFFu;
+            bitonic_lanes<4>(x, lane);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, A, B, C, D, sorted, spos,
+                            sfwd, due, ctl);
         } else {
             // long range (dense cell or hash collision): rank by counting
             for (uint32_t c0 = 0; c0 < L; c0 += 32) {

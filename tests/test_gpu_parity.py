@@ -204,12 +204,15 @@ def test_hash_collisions(native, oracle):
     assert len(np.unique(r["keys"])) < len({tuple(np.floor(p / 4)) for p in w[:, :3]})
 
 
-def test_dense_cell_and_long_ranges(native, oracle):
-    # 300 birds in one 4 m cell: bucket range > 32 takes the counting sort path
-    rng = np.random.default_rng(2)
-    pos = rng.uniform(0.0, 4.0, size=(300, 3)) + np.array([40.0, 40.0, 100.0])
+@pytest.mark.parametrize("per_cell", [45, 100, 300])
+def test_dense_cell_and_long_ranges(native, oracle, per_cell):
+    # one crowded 4 m cell: bucket ranges of 33-64 and 65-128 birds take the
+    # register bitonic sorts, longer ones the counting sort
+    rng = np.random.default_rng(per_cell)
+    pos = rng.uniform(0.0, 4.0, size=(per_cell, 3)) + np.array([40.0, 40.0, 100.0])
     w = np.stack([bird(p, radius=0.6, next_decision=rng.uniform(0, 0.01)) for p in pos]).astype(np.float32)
-    assert_step_parity(native, oracle, w)
+    extra = oracle.scatter(1500, per_cell)
+    assert_step_parity(native, oracle, np.concatenate([w, extra]))
 
 
 def test_wide_radii_take_the_cell_walk_and_brute_force_paths(native, oracle):
@@ -234,8 +237,9 @@ def test_steps_are_deterministic(native):
 def test_grid_reporting_and_production_steps_agree_bit_for_bit(native):
     """A step that reports its grid places bucket runs at the canonical dense
     offsets; a production step places them from per-flock cursors. Results
-    must not depend on the placement."""
-    for n, seed in [(50_000, 2), (3_000, 8)]:
+    must not depend on the placement. Above 2M birds the production step also
+    uses a larger bucket table than the canonical 2^22."""
+    for n, seed in [(50_000, 2), (3_000, 8), (3_000_000, 4)]:
         w = native.generate(n, seed)
         a = native.Flock(w)
         a.step_debug()
