@@ -69,6 +69,25 @@ __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
     return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
 }
 
+// Bucket of a cell in a production step (one that reports no grid). The
+// reference hash above sends about a third of a compact flock's cells to a
+// bucket shared with another cell (its XOR of products collides on the cell
+// lattice), which costs decide a second cell of candidates each time. Here the
+// cell's coordinates are taken modulo a 2^bx x 2^by x 2^bz lattice (bx + by +
+// bz = log2 buckets, x fastest): cells of a flock narrower than the lattice in
+// every axis (512 m per axis from 2^21 buckets) never share a bucket, and
+// neighbouring cells along x get neighbouring buckets. Wider flocks wrap, and
+// a cell then shares its bucket with its lattice translate; results do not
+// depend on which cells share buckets.
+__device__ __forceinline__ uint32_t lattice_bucket(int cx, int cy, int cz, uint32_t buckets) {
+    const uint32_t k = 31u - (uint32_t)__clz(buckets);  // buckets = 2^k, k >= 16
+    const uint32_t bx = (k + 2u) / 3u, by = (k + 1u - bx) >> 1, bz = k - bx - by;
+    const uint32_t x = (uint32_t)cx & ((1u << bx) - 1u);
+    const uint32_t y = (uint32_t)cy & ((1u << by) - 1u);
+    const uint32_t z = (uint32_t)cz & ((1u << bz) - 1u);
+    return x | (y << bx) | (z << (bx + by));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -90,6 +109,11 @@ __device__ __forceinline__ int find_flock_b(const FlockDesc* __restrict__ fl, in
         if (__ldg(&fl[mid].bbase) <= b) lo = mid; else hi = mid - 1;
     }
     return lo;
+}
+
+// Slot - view index of a flock's birds in buffer p (wraps modulo 2^32).
+__device__ __forceinline__ uint32_t view_shift(uint32_t sbase, uint32_t vbase, uint32_t p, uint32_t cap) {
+    return p * cap + sbase - vbase;
 }
 
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {

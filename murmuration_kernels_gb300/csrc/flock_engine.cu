@@ -13,13 +13,16 @@
 //                 zeroes the histogram for the next step. Bounded waits.
 //   k_scatter     bird -> slot in its bucket's range (arrival order).
 //   k_segsort     one warp per occupied bucket sorts its range by bird index
-//                 (the canonical stable order), writes the cell-ordered float4
-//                 view (pos+id, forward direction) and the deciding-bird list.
+//                 (the canonical stable order) and moves those birds' state
+//                 into the other of the flock's two state buffers in that
+//                 order; it also writes each bird's unit heading and the
+//                 deciding-bird list.
 //   k_decide      one warp per deciding bird: the 2R neighbourhood's buckets
 //                 are deduplicated with __match_any_sync, lanes sweep each
 //                 bucket's contiguous float4 range, and warp shuffles reduce.
-//   k_integrate   banked flight, streaming float4; its last block advances the
-//                 flock clocks and resets the step counters.
+//   k_integrate   banked flight, streaming float4 over the reordered buffer;
+//                 its last block advances the flock clocks, makes the
+//                 reordered buffer current and resets the step counters.
 //
 // Exactness: the file is compiled with -fmad=false, and the expressions that
 // decide set membership use explicit round-to-nearest intrinsics, so cell
@@ -98,10 +101,10 @@ Engine::~Engine() {
     if (stream_) cudaStreamSynchronize(stream_);
     if (copy_) cudaStreamSynchronize(copy_);
     free_graphs();
-    dfree(A_); dfree(B_); dfree(C_); dfree(D_);
+    dfree(ar_.A); dfree(ar_.B); dfree(ar_.C); dfree(ar_.D); dfree(ar_.id);
     dfree(table_d_);
-    dfree(key_); dfree(arrival_); dfree(tmp_); dfree(sorted_); dfree(occ_); dfree(due_);
-    dfree(spos_); dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_);
+    dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
+    dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
     if (copy_) cudaStreamDestroy(copy_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -114,10 +117,11 @@ void Engine::free_graphs() {
 }
 
 size_t Engine::bytes_for(uint32_t n) {
-    // state 64 B + scratch (key, arrival, tmp, sorted, occ 4 B each; due 8 B;
-    // spos, sfwd 16 B each) + buckets (counts 4 B + offsets 4 B + status/4096)
+    // state 2 x 68 B (two buffers) + scratch (key, arrival, occ 4 B each; tmp
+    // 8 B; due record 48 B; heading 16 B) + buckets (counts 4 B + offsets 4 B +
+    // status/4096)
     const size_t b = production_buckets(n);
-    return (size_t)n * (64 + 20 + 48 + 32) + b * 8 + (b / SCAN_TILE) * 8 + 256;
+    return (size_t)n * (136 + 84) + b * 8 + (b / SCAN_TILE) * 8 + 256;
 }
 
 void Engine::set_shape(const LaunchShape& s) {
@@ -133,20 +137,32 @@ void Engine::set_shape(const LaunchShape& s) {
 
 void Engine::ensure_arena(uint32_t need) {
     if (need <= cap_) return;
+    // both buffers of a field share one allocation indexed by 32-bit slots
+    if (need >= (1u << 31)) throw Error{-5, "arena above 2^31 birds"};
     uint32_t ncap = std::max<uint32_t>(need, cap_ ? cap_ + cap_ / 2 : need);
+    ncap = std::min<uint32_t>(ncap, (1u << 31) - 1);
     size_t acct = 0;
-    float4 *a = dalloc<float4>(ncap, &acct), *b = dalloc<float4>(ncap, &acct), *c = dalloc<float4>(ncap, &acct),
-           *d = dalloc<float4>(ncap, &acct);
+    Arena na{};
+    na.cap = ncap;
+    na.A = dalloc<float4>((size_t)ncap * 2, &acct);
+    na.B = dalloc<float4>((size_t)ncap * 2, &acct);
+    na.C = dalloc<float4>((size_t)ncap * 2, &acct);
+    na.D = dalloc<float4>((size_t)ncap * 2, &acct);
+    na.id = dalloc<uint32_t>((size_t)ncap * 2, &acct);
     if (used_) {
-        FLK_CUDA(cudaMemcpyAsync(a, A_, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
-        FLK_CUDA(cudaMemcpyAsync(b, B_, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
-        FLK_CUDA(cudaMemcpyAsync(c, C_, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
-        FLK_CUDA(cudaMemcpyAsync(d, D_, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
+        for (size_t p = 0; p < 2; ++p) {
+            const size_t o = p * cap_, n = p * ncap;
+            FLK_CUDA(cudaMemcpyAsync(na.A + n, ar_.A + o, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
+            FLK_CUDA(cudaMemcpyAsync(na.B + n, ar_.B + o, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
+            FLK_CUDA(cudaMemcpyAsync(na.C + n, ar_.C + o, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
+            FLK_CUDA(cudaMemcpyAsync(na.D + n, ar_.D + o, (size_t)used_ * 16, cudaMemcpyDeviceToDevice, stream_));
+            FLK_CUDA(cudaMemcpyAsync(na.id + n, ar_.id + o, (size_t)used_ * 4, cudaMemcpyDeviceToDevice, stream_));
+        }
         FLK_CUDA(cudaStreamSynchronize(stream_));
     }
-    dev_bytes_ -= (size_t)cap_ * 64;
-    dfree(A_); dfree(B_); dfree(C_); dfree(D_);
-    A_ = a; B_ = b; C_ = c; D_ = d;
+    dev_bytes_ -= (size_t)cap_ * 136;
+    dfree(ar_.A); dfree(ar_.B); dfree(ar_.C); dfree(ar_.D); dfree(ar_.id);
+    ar_ = na;
     dev_bytes_ += acct;
     cap_ = ncap;
     free_graphs();
@@ -183,7 +199,7 @@ int Engine::add_flock(uint32_t n, float time, const float* words) {
         }
         FLK_CUDA(cudaMemcpyAsync(staging_, words, bytes, cudaMemcpyHostToDevice, stream_));
         const int blocks = std::min<uint32_t>((n + 255) / 256, (uint32_t)num_sms_ * 8);
-        k_unpack<<<blocks, 256, 0, stream_>>>(staging_, n, sbase, A_, B_, C_, D_);
+        k_unpack<<<blocks, 256, 0, stream_>>>(staging_, n, sbase, ar_);  // buffer 0
         FLK_CUDA(cudaGetLastError());
     }
     Slot s;
@@ -228,6 +244,7 @@ void Engine::sync_times() {
         Slot& s = slots_[table_ids_[k]];
         s.time = t[k].time;
         s.remaining = t[k].remaining;
+        s.parity = t[k].parity;
     }
     table_h_ = t;
 }
@@ -304,7 +321,7 @@ int Engine::add_flock_async(uint32_t n, float time, const float* words) {
         s.buckets = buckets_for(n);
         FLK_CUDA(cudaStreamWaitEvent(stream_, landed, 0));
         const int blocks = std::min<uint32_t>((n + 255) / 256, (uint32_t)num_sms_ * 8);
-        k_unpack<<<blocks, 256, 0, stream_>>>(stage, n, sbase, A_, B_, C_, D_);
+        k_unpack<<<blocks, 256, 0, stream_>>>(stage, n, sbase, ar_);  // buffer 0
         FLK_CUDA(cudaGetLastError());
         FLK_CUDA(cudaFreeAsync(stage, stream_));
         FLK_CUDA(cudaEventDestroy(landed));
@@ -325,7 +342,7 @@ void Engine::read_flock_async(int id, float* time, float* words, cudaEvent_t don
         float* stage = nullptr;
         FLK_CUDA(cudaMallocAsync((void**)&stage, bytes, stream_));
         const int blocks = std::min<uint32_t>((s.n + 255) / 256, (uint32_t)num_sms_ * 8);
-        k_pack<<<blocks, 256, 0, stream_>>>(stage, s.n, s.sbase, A_, B_, C_, D_);
+        k_pack<<<blocks, 256, 0, stream_>>>(stage, s.n, (s.parity & 1u) * cap_ + s.sbase, ar_);
         FLK_CUDA(cudaGetLastError());
         cudaEvent_t packed;
         FLK_CUDA(cudaEventCreateWithFlags(&packed, cudaEventDisableTiming));
@@ -353,7 +370,7 @@ void Engine::read_flock(int id, float* time, float* words) {
         staging_cap_ = bytes;
     }
     const int blocks = std::min<uint32_t>((s.n + 255) / 256, (uint32_t)num_sms_ * 8);
-    k_pack<<<blocks, 256, 0, stream_>>>(staging_, s.n, s.sbase, A_, B_, C_, D_);
+    k_pack<<<blocks, 256, 0, stream_>>>(staging_, s.n, (s.parity & 1u) * cap_ + s.sbase, ar_);
     FLK_CUDA(cudaGetLastError());
     FLK_CUDA(cudaMemcpyAsync(words, staging_, bytes, cudaMemcpyDeviceToHost, stream_));
     FLK_CUDA(cudaStreamSynchronize(stream_));
@@ -489,6 +506,7 @@ void Engine::rebuild_table(bool grid_output) {
         d.buckets = grid_output ? s.buckets : production_buckets(s.n);
         d.remaining = s.remaining;
         d.time = s.time;
+        d.parity = s.parity;
         t.push_back(d);
         ids.push_back((int)k);
         V += s.n;
@@ -518,16 +536,15 @@ void Engine::rebuild_table(bool grid_output) {
 void Engine::ensure_scratch() {
     if (V_ > scratch_V_ || !key_) {
         const uint32_t nv = std::max<uint32_t>(V_, scratch_V_ + scratch_V_ / 2);
-        dev_bytes_ -= (size_t)scratch_V_ * (20 + 48 + 32);
-        dfree(key_); dfree(arrival_); dfree(tmp_); dfree(sorted_); dfree(occ_); dfree(due_);
-        dfree(spos_); dfree(sfwd_); dfree(sets_);
+        dev_bytes_ -= (size_t)scratch_V_ * 84;
+        if (sets_) dev_bytes_ -= (size_t)scratch_V_ * 32;
+        dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
+        dfree(sfwd_); dfree(sets_);
         key_ = dalloc<uint32_t>(nv, &dev_bytes_);
         arrival_ = dalloc<uint32_t>(nv, &dev_bytes_);
-        tmp_ = dalloc<uint32_t>(nv, &dev_bytes_);
-        sorted_ = dalloc<uint32_t>(nv, &dev_bytes_);
+        tmp_ = dalloc<unsigned long long>(nv, &dev_bytes_);
         occ_ = dalloc<uint32_t>(nv, &dev_bytes_);
         due_ = dalloc<DueRec>(nv, &dev_bytes_);
-        spos_ = dalloc<float4>(nv, &dev_bytes_);
         sfwd_ = dalloc<float4>(nv, &dev_bytes_);
         scratch_V_ = nv;
         free_graphs();
@@ -559,7 +576,10 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
     const int sblocks = pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256);
     const uint32_t ntiles = Btot_ / SCAN_TILE;
     if (ev) FLK_CUDA(cudaEventRecord(ev[0], stream_));
-    k_hash_count<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, key_, arrival_, counts_, occ_, ctl_);
+    if (sets)  // a grid-reporting step: the reference's cell hash
+        k_hash_count<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, counts_, occ_, ctl_);
+    else
+        k_hash_count<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, counts_, occ_, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
     if (sets) {
         // a step that reports its grid builds the canonical dense offsets
@@ -570,9 +590,9 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
                                                                                            counts_, offsets_, ctl_);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
-    k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, key_, arrival_, offsets_, tmp_, ctl_);
+    k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
-        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, A_, B_, C_, D_, sorted_, spos_, sfwd_, due_);
+        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, ar_, sfwd_, due_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
     // per-warp hit queue + reduced birds awaiting their epilogue
@@ -580,14 +600,12 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
                           (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                       counts_, spos_, sfwd_, B_, C_, D_,
-                                                                       radius_table_, sets_);
+                                                                       counts_, ar_, sfwd_, radius_table_, sets_);
     else
         k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                        counts_, spos_, sfwd_, B_, C_, D_,
-                                                                        radius_table_, nullptr);
+                                                                        counts_, ar_, sfwd_, radius_table_, nullptr);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
-    k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, A_, B_, C_, counts_, occ_, ctl_);
+    k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, counts_, occ_, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
 }
 
@@ -676,21 +694,38 @@ void Engine::step_debug(std::vector<GridDebug>* out) {
     enqueue_step(true);
     FLK_CUDA(cudaGetLastError());
     FLK_CUDA(cudaStreamSynchronize(stream_));
-    std::vector<uint32_t> key(V_), offs((size_t)Btot_ + 1), sorted(V_), sets((size_t)V_ * 8);
+    std::vector<uint32_t> key(V_), offs((size_t)Btot_ + 1), sets((size_t)V_ * 8);
     FLK_CUDA(cudaMemcpy(key.data(), key_, (size_t)V_ * 4, cudaMemcpyDeviceToHost));
     FLK_CUDA(cudaMemcpy(offs.data(), offsets_, ((size_t)Btot_ + 1) * 4, cudaMemcpyDeviceToHost));
-    FLK_CUDA(cudaMemcpy(sorted.data(), sorted_, (size_t)V_ * 4, cudaMemcpyDeviceToHost));
     FLK_CUDA(cudaMemcpy(sets.data(), sets_, (size_t)V_ * 8 * 4, cudaMemcpyDeviceToHost));
+    // bird index per slot in both buffers: the step read buf[parity] (keys are
+    // per old slot) and wrote buf[parity ^ 1] (sorted order, sets per new slot)
+    std::vector<uint32_t> ids[2];
+    for (int k = 0; k < 2; ++k) {
+        ids[k].resize(used_);
+        if (used_)
+            FLK_CUDA(cudaMemcpy(ids[k].data(), ar_.id + (size_t)k * cap_, (size_t)used_ * 4, cudaMemcpyDeviceToHost));
+    }
     out->clear();
     for (const FlockDesc& d : before) {
+        const std::vector<uint32_t>& oid = ids[d.parity & 1u];
+        const std::vector<uint32_t>& nid = ids[(d.parity & 1u) ^ 1u];
         GridDebug g;
-        g.keys.resize(d.n);
-        for (uint32_t i = 0; i < d.n; ++i) g.keys[i] = key[d.vbase + i] - d.bbase;
+        g.keys.assign(d.n, 0);
+        g.sets.assign((size_t)d.n * 8, 0);
+        g.sorted.resize(d.n);
+        for (uint32_t i = 0; i < d.n; ++i) {
+            const uint32_t bo = oid[d.sbase + i], bn = nid[d.sbase + i];
+            if (bo >= d.n || bn >= d.n) throw Error{-6, "bird index out of range in step_debug"};
+            g.keys[bo] = key[d.vbase + i] - d.bbase;
+            g.sorted[i] = bn;  // view index vbase + i holds bird bn
+            std::copy(sets.begin() + (size_t)(d.vbase + i) * 8, sets.begin() + (size_t)(d.vbase + i + 1) * 8,
+                      g.sets.begin() + (size_t)bn * 8);
+        }
         g.offsets.resize((size_t)d.buckets + 1);
         const uint32_t o0 = offs[d.bbase];
         for (uint32_t b = 0; b <= d.buckets; ++b) g.offsets[b] = offs[(size_t)d.bbase + b] - o0;
-        g.sorted.assign(sorted.begin() + o0, sorted.begin() + o0 + d.n);
-        g.sets.assign(sets.begin() + (size_t)d.vbase * 8, sets.begin() + (size_t)(d.vbase + d.n) * 8);
+        if (o0 != d.vbase) throw Error{-6, "grid offsets of a flock do not start at its view base"};
         out->push_back(std::move(g));
     }
     sync_times();  // clocks and countdowns from the device table

@@ -23,6 +23,25 @@ struct FlockDesc {
     uint32_t remaining;  // steps still to run; 0 = idle this step
     float time;          // world clock (f32, as the reference keeps it)
     uint32_t cursor;     // next free slot of the flock's view region (bucket allocation; reset per step)
+    uint32_t parity;     // which of the two state buffers holds the flock's current state
+    uint32_t pad[3];
+};
+
+// The arena's state, two copies: buffer p of each field occupies entries
+// [p * cap, (p + 1) * cap). A = position, roll; B = velocity, spin; C =
+// steering, radius; D = next_decision, neighbours (u32 bits), centrality;
+// id = the bird's index in its flock. Each step reads a flock's state from
+// buffer `parity` and writes it, reordered by cell, into buffer parity ^ 1, so
+// consecutive slots hold birds of the same cell (coherent gathers,
+// warp-aggregated atomics, and the candidate view for decide is the state
+// itself). Slot of view index v of a flock in buffer p: v + p * cap + sbase - vbase.
+struct Arena {
+    float4* A;
+    float4* B;
+    float4* C;
+    float4* D;
+    uint32_t* id;
+    uint32_t cap;
 };
 
 // Step-control block in device memory: per-step counters (reset by the last
@@ -47,7 +66,7 @@ struct StepCtl {
 struct __align__(16) DueRec {
     float4 pr;  // position xyz, radius
     float4 fk;  // unit heading xyz, index in the cell-ordered view (u32 bits)
-    uint4 fl;   // arena slot, bucket base, bucket count, virtual index
+    uint4 fl;   // slot in the reordered buffer, bucket base, bucket count, slot - view index of that buffer
 };
 
 enum DeviceError : uint32_t {
@@ -137,6 +156,7 @@ public:
 private:
     struct Slot {
         uint32_t n = 0, sbase = 0, buckets = 0, remaining = 0;
+        uint32_t parity = 0;  // buffer holding the current state
         float time = 0.f;
         bool live = false;
     };
@@ -157,7 +177,7 @@ private:
 
     // arena (storage order)
     uint32_t cap_ = 0, used_ = 0;
-    float4 *A_ = nullptr, *B_ = nullptr, *C_ = nullptr, *D_ = nullptr;
+    Arena ar_{};  // two state buffers, cap_ birds each
     std::vector<Slot> slots_;
     std::vector<std::pair<uint32_t, uint32_t>> free_ranges_;  // (sbase, n) holes
 
@@ -173,9 +193,10 @@ private:
 
     // scratch (virtual / sorted order)
     uint32_t scratch_V_ = 0, scratch_B_ = 0;
-    uint32_t *key_ = nullptr, *arrival_ = nullptr, *tmp_ = nullptr, *sorted_ = nullptr, *occ_ = nullptr;
+    uint32_t *key_ = nullptr, *arrival_ = nullptr, *occ_ = nullptr;
+    unsigned long long* tmp_ = nullptr;  // sort keys: bird << 32 | view index
     DueRec* due_ = nullptr;
-    float4 *spos_ = nullptr, *sfwd_ = nullptr;  // cell-ordered view read by decide
+    float4* sfwd_ = nullptr;  // unit heading per view index (read by decide)
     uint32_t *counts_ = nullptr, *offsets_ = nullptr;
     unsigned long long* status_ = nullptr;
     uint32_t* sets_ = nullptr;  // 8 per virtual bird, debug only

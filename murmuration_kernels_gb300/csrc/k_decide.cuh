@@ -9,8 +9,10 @@
 // with the reference's exact cell check (cuda/flock.cu:219-221), and a box
 // wider than the flock itself sweeps the flock's whole range.
 //
-// Each bucket's birds are contiguous in the cell-ordered float4 view, so the
-// lanes of a warp read one coalesced 512 B run per cell. The sweep is split in
+// Each bucket's birds are contiguous in the flock's state, which the sort
+// pass has just written in cell order (view index t lives in slot t + shift of
+// the reordered buffer), so the lanes of a warp read one coalesced 512 B run
+// of positions per cell. The sweep is split in
 // two: the cheap phase computes d2 for every candidate and appends the indices
 // of those within 2R to a per-warp queue in shared memory (ballot + popc);
 // whenever 32 hits are queued, the whole warp processes them together in the
@@ -48,16 +50,20 @@ __device__ __forceinline__ uint32_t set_mix(uint32_t j) {
 
 // Bucket range [s, e) of bucket b: its start (offsets) and length (counts). An
 // empty bucket's start is stale and never used; an inconsistent range (only
-// possible if the grid build gave up) is recorded and treated as empty.
+// possible if the grid build gave up) is recorded and treated as empty. The
+// range's slots [s + shift, e + shift) must also lie inside the state arrays
+// (lim = 2 * cap entries).
 __device__ __forceinline__ void bucket_range(const uint32_t* __restrict__ offsets,
                                              const uint32_t* __restrict__ counts, uint32_t b, uint32_t V,
-                                             StepCtl* __restrict__ ctl, uint32_t& s, uint32_t& e) {
+                                             uint32_t shift, uint32_t lim, StepCtl* __restrict__ ctl, uint32_t& s,
+                                             uint32_t& e) {
     const uint32_t c = __ldg(&counts[b]);
     s = __ldg(&offsets[b]);
     e = s + c;
+    const uint32_t ss = s + shift;
     if (c == 0) {
         e = s = 0;
-    } else if (e < s || e > V) {
+    } else if (e < s || e > V || ss + c < ss || ss + c > lim) {
         atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
         e = s = 0;
     }
@@ -68,8 +74,10 @@ struct Sweep {
     f3 p, fi;
     float r2, c2;
     uint32_t self;
-    const float4* __restrict__ spos;
-    const float4* __restrict__ sfwd;
+    uint32_t shift;                   // slot - view index of the bird's flock
+    const float4* __restrict__ pos;   // state: position, roll (by slot)
+    const uint32_t* __restrict__ bid;  // state: bird index (by slot)
+    const float4* __restrict__ sfwd;  // unit headings (by view index)
     uint32_t* q;  // this warp's 64-entry hit queue (shared memory)
     uint32_t qn;  // entries queued (warp-uniform)
     Acc a;
@@ -78,14 +86,14 @@ struct Sweep {
 // Expensive phase for one hit t (d2 <= c2 already established).
 template <bool SETS>
 __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
-    const float4 q = __ldg(&w.spos[t]);
+    const float4 q = __ldg(&w.pos[t + w.shift]);
     const f3 d = mk(__fsub_rn(q.x, w.p.x), __fsub_rn(q.y, w.p.y), __fsub_rn(q.z, w.p.z));
     const float d2 = dot(d, d);
     const float dist = __fsqrt_rn(d2);
     const f3 dh = dvs(d, fmaxf(dist, 1e-6f));
     w.a.csum = add(w.a.csum, dh);
     w.a.n_g += 1;
-    const uint32_t j = __float_as_uint(q.w);
+    const uint32_t j = SETS ? __ldg(&w.bid[t + w.shift]) : 0u;
     if (SETS) w.a.h_g += set_mix(j);
     if (d2 > w.r2) return;
     w.a.n_all += 1;
@@ -145,7 +153,7 @@ __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32
     for (uint32_t base = sc; base < ec; base += 32) {
         const uint32_t t = base + lane;
         bool hit = false;
-        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.spos[t]), cx, cy, cz);
+        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.pos[t + w.shift]), cx, cy, cz);
         enqueue<SETS>(w, hit, t, lane);
     }
 }
@@ -180,8 +188,8 @@ __device__ __forceinline__ void sweep_ranges(Sweep& w, uint32_t km, uint32_t s, 
         const bool vA = tA < e0 && tA != w.self;
         const bool vB = have1 && tB < e1 && tB != w.self;
         float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
-        if (vA) qA = __ldg(&w.spos[tA]);
-        if (vB) qB = __ldg(&w.spos[tB]);
+        if (vA) qA = __ldg(&w.pos[tA + w.shift]);
+        if (vB) qB = __ldg(&w.pos[tB + w.shift]);
         const bool hA = vA && near<false>(w, qA, 0, 0, 0);
         const bool hB = vB && near<false>(w, qB, 0, 0, 0);
         enqueue<SETS>(w, hA, tA, lane);
@@ -255,17 +263,19 @@ struct WarpSmem {
     uint32_t queue[64];
     float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
     uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
-    uint32_t st[32];       // arena slot of the bird
-    uint32_t vix[32];      // virtual index (set summaries)
+    uint32_t st[32];       // slot of the bird in the reordered buffer
+    uint32_t vix[32];      // view index (set summaries)
     float pz[32];          // height (roost pull)
 };
 
 // Finishes bird `slot` of the warp's batch (model.rs:95-144), one lane per bird.
 template <bool SETS>
-__device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot, const float4* __restrict__ Bv,
-                                         float4* __restrict__ C, float4* __restrict__ D,
+__device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot, const Arena& ar,
                                          const float* __restrict__ rtab, uint32_t* __restrict__ sets) {
     const uint32_t st = m.st[slot];
+    const float4* __restrict__ Bv = ar.B;
+    float4* __restrict__ C = ar.C;
+    float4* __restrict__ D = ar.D;
     const f3 sep = mk(m.red[0][slot], m.red[1][slot], m.red[2][slot]);
     const f3 coh = mk(m.red[3][slot], m.red[4][slot], m.red[5][slot]);
     const f3 align = mk(m.red[6][slot], m.red[7][slot], m.red[8][slot]);
@@ -299,6 +309,13 @@ __device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot,
 #define FLK_DECIDE_MIN_BLOCKS 4
 #endif
 
+// Bucket of cell (cx, cy, cz): SETS steps report their grid and use the
+// reference hash; production steps use the lattice index.
+template <bool SETS>
+__device__ __forceinline__ uint32_t bucket_of(int cx, int cy, int cz, uint32_t buckets) {
+    return SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u)) : lattice_bucket(cx, cy, cz, buckets);
+}
+
 // Dynamic shared memory: one WarpSmem<SETS> per warp.
 template <bool SETS>
 __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const FlockDesc* __restrict__ fl, int nfl,
@@ -306,10 +323,8 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                                                                       const DueRec* __restrict__ due,
                                                                       const uint32_t* __restrict__ offsets,
                                                                       const uint32_t* __restrict__ counts,
-                                                                      const float4* __restrict__ spos,
+                                                                      Arena ar,
                                                                       const float4* __restrict__ sfwd,
-                                                                      const float4* __restrict__ Bv,
-                                                                      float4* __restrict__ C, float4* __restrict__ D,
                                                                       const float* __restrict__ rtab,
                                                                       uint32_t* __restrict__ sets) {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -321,7 +336,8 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
     uint32_t cand = 0, pairs = 0, slot = 0;
 
     Sweep w;
-    w.spos = spos;
+    w.pos = ar.A;
+    w.bid = ar.id;
     w.sfwd = sfwd;
     w.q = m.queue;
     w.qn = 0;
@@ -330,6 +346,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         const DueRec rec = due[e];  // everything the setup needs, one place
         const uint32_t k = __float_as_uint(rec.fk.w);
         const uint32_t st = rec.fl.x, bbase = rec.fl.y, buckets = rec.fl.z;
+        w.shift = rec.fl.w;
         const float r = rec.pr.w;
         w.p = mk(rec.pr.x, rec.pr.y, rec.pr.z);
         w.fi = mk(rec.fk.x, rec.fk.y, rec.fk.z);
@@ -350,7 +367,6 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         const bool wide = nxl > (1 << 20) || nyl > (1 << 20) || nzl > (1 << 20);
         const long long ncell = wide ? (1ll << 62) : nxl * nyl * nzl;
         const int nx = (int)nxl, ny = (int)nyl;
-        const uint32_t mask = buckets - 1u;
 
         w.a.sep = w.a.coh = w.a.align = w.a.csum = mk(0.f, 0.f, 0.f);
         w.a.n_all = w.a.n_star = w.a.n_align = w.a.n_g = 0;
@@ -369,7 +385,7 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                 const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
                 const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                 valid = dx * dx + dy * dy + dz * dz <= reach2;
-                b = bbase + (cell_hash(cx, cy, cz) & mask);
+                b = bbase + bucket_of<SETS>(cx, cy, cz, buckets);
             }
             const uint32_t vm = __ballot_sync(FULL, valid);
             bool keep = false;
@@ -378,14 +394,15 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                 keep = (int)lane == __ffs(peers) - 1;
             }
             uint32_t s = 0, en = 0;
-            if (keep) bucket_range(offsets, counts, b, V, ctl, s, en);
+            if (keep) bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
             cand += en - s;
             sweep_ranges<SETS>(w, __ballot_sync(FULL, en > s), s, en, lane);
         } else {
             // the flock's own view region [vbase, vbase + n)
-            const FlockDesc* fd = &fl[find_flock_v(fl, nfl, rec.fl.w)];
+            const FlockDesc* fd = &fl[find_flock_v(fl, nfl, k)];
             uint32_t f0 = __ldg(&fd->vbase), f1 = f0 + __ldg(&fd->n);
-            if (f1 < f0 || f1 > V) f1 = f0 = 0;
+            const uint32_t sf = f0 + w.shift;
+            if (f1 < f0 || f1 > V || sf + (f1 - f0) < sf || sf + (f1 - f0) > 2u * ar.cap) f1 = f0 = 0;
             if (ncell * 16 >= (long long)(f1 - f0)) {
                 // very wide reach: brute force over the flock's own range
                 if (lane == 0) cand += f1 - f0;
@@ -408,7 +425,8 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
                         const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                         valid = dx * dx + dy * dy + dz * dz <= reach2;
                         if (valid) {
-                            bucket_range(offsets, counts, bbase + (cell_hash(cx, cy, cz) & mask), V, ctl, s, en);
+                            bucket_range(offsets, counts, bbase + bucket_of<SETS>(cx, cy, cz, buckets), V, w.shift,
+                                         2u * ar.cap, ctl, s, en);
                             valid = en > s;
                         }
                     }
@@ -449,19 +467,19 @@ __global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const Flo
         }
         if (lane == 0) {
             m.st[slot] = st;
-            m.vix[slot] = rec.fl.w;
+            m.vix[slot] = k;
             m.pz[slot] = p.z;
         }
         if (++slot == 32) {
             __syncwarp();
-            epilogue<SETS>(m, lane, Bv, C, D, rtab, sets);
+            epilogue<SETS>(m, lane, ar, rtab, sets);
             __syncwarp();
             slot = 0;
         }
     }
     if (slot) {
         __syncwarp();
-        if (lane < slot) epilogue<SETS>(m, lane, Bv, C, D, rtab, sets);
+        if (lane < slot) epilogue<SETS>(m, lane, ar, rtab, sets);
     }
     // per-warp totals straight to the counters (no block barrier)
     const uint32_t cand_w = __reduce_add_sync(FULL, cand), pairs_w = __reduce_add_sync(FULL, pairs);

@@ -1,34 +1,47 @@
 // Passes 1-4 of the step: .flk words <-> arena, cell key + histogram, the
 // single-pass decoupled look-back scan, scatter by arrival rank, and the
-// per-bucket stable sort that writes the cell-ordered view and the
-// deciding-bird list (reference cuda/flock.cu:118-179, made stable).
+// per-bucket stable sort that moves each flock's state into cell order and
+// writes the deciding-bird list (reference cuda/flock.cu:118-179, made stable).
+//
+// A flock's state lives in one of two buffers (FlockDesc::parity). A step
+// reads it from buffer parity, in the cell order of the previous step, and
+// the sort writes it to buffer parity ^ 1 in this step's cell order; decide
+// and integrate then work on that copy, and integrate's last block flips the
+// parity. Because consecutive slots already hold birds of one cell, the
+// histogram's atomics aggregate within a warp, the scatter writes runs, and
+// the sort's gathers read mostly contiguous runs.
 #pragma once
 
 #include "device_common.cuh"
 
 namespace flk {
 
+
 // ---------------------------------------------------------------------------
 // .flk words <-> arena (A = pos,roll  B = vel,spin  C = steer,radius  D = next,nb,cen)
 // ---------------------------------------------------------------------------
-__global__ void k_unpack(const float* __restrict__ w, uint32_t n, uint32_t sbase, float4* A, float4* B, float4* C,
-                         float4* D) {
+// Loads bird i of a flock into slot base + i (bird order).
+__global__ void k_unpack(const float* __restrict__ w, uint32_t n, uint32_t base, Arena s) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float* r = w + (size_t)i * WORDS;
-        const uint32_t s = sbase + i;
-        A[s] = make_float4(r[0], r[1], r[2], r[6]);
-        B[s] = make_float4(r[3], r[4], r[5], r[7]);
-        C[s] = make_float4(r[9], r[10], r[11], r[8]);
-        D[s] = make_float4(r[12], r[13], r[14], 0.f);
+        const uint32_t k = base + i;
+        s.A[k] = make_float4(r[0], r[1], r[2], r[6]);
+        s.B[k] = make_float4(r[3], r[4], r[5], r[7]);
+        s.C[k] = make_float4(r[9], r[10], r[11], r[8]);
+        s.D[k] = make_float4(r[12], r[13], r[14], 0.f);
+        s.id[k] = i;
     }
 }
 
-__global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t sbase, const float4* A, const float4* B,
-                       const float4* C, const float4* D) {
+// Writes the flock held in slots [base, base + n) (any order) back as .flk
+// words in bird order.
+__global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t base, Arena s) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float* r = w + (size_t)i * WORDS;
-        const uint32_t s = sbase + i;
-        const float4 a = A[s], b = B[s], c = C[s], d = D[s];
+        const uint32_t k = base + i;
+        const uint32_t bird = s.id[k];
+        if (bird >= n) continue;  // never for a valid arena
+        float* r = w + (size_t)bird * WORDS;
+        const float4 a = s.A[k], b = s.B[k], c = s.C[k], d = s.D[k];
         r[0] = a.x; r[1] = a.y; r[2] = a.z;
         r[3] = b.x; r[4] = b.y; r[5] = b.z;
         r[6] = a.w; r[7] = b.w; r[8] = c.w;
@@ -40,26 +53,39 @@ __global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t sbase, const 
 // ---------------------------------------------------------------------------
 // pass 1: cell key + histogram (warp-aggregated atomics)
 // ---------------------------------------------------------------------------
+// LATTICE: production bucket function (lattice_bucket); otherwise the
+// reference's cell hash, whose keys a grid-reporting step returns.
+// Each CTA takes 256 consecutive view indices per iteration. Bucket counts
+// use one atomic per distinct bucket of a warp; the occupied-bucket list gets
+// one atomic per CTA iteration (the first-seen buckets of all eight warps are
+// placed from a shared-memory prefix), so the single list counter is not hit
+// once per warp.
+template <bool LATTICE>
 __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
-                                                    const float4* __restrict__ A, uint32_t* __restrict__ key,
+                                                    Arena ar, uint32_t* __restrict__ key,
                                                     uint32_t* __restrict__ arrival, uint32_t* __restrict__ counts,
                                                     uint32_t* __restrict__ occ, StepCtl* __restrict__ ctl) {
-    const uint32_t lane = threadIdx.x & 31;
+    __shared__ uint32_t s_first[2][8];  // per warp: first-seen buckets, then their start in occ
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < V; v0 += stride) {
-        const uint32_t v = v0 + lane;
+    uint32_t it = 0;
+    for (uint32_t blk = blockIdx.x * blockDim.x; blk < V; blk += stride, it ^= 1u) {
+        const uint32_t v = blk + threadIdx.x;
         bool act = false;
         uint32_t b = 0;
         if (v < V) {
             const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
             if (__ldg(&d->remaining)) {
-                const float4 p = A[__ldg(&d->sbase) + (v - __ldg(&d->vbase))];
-                b = __ldg(&d->bbase) + (cell_hash(cell1(p.x), cell1(p.y), cell1(p.z)) & (__ldg(&d->buckets) - 1u));
+                const float4 p = ar.A[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
+                const int cx = cell1(p.x), cy = cell1(p.y), cz = cell1(p.z);
+                const uint32_t nb = __ldg(&d->buckets);
+                b = __ldg(&d->bbase) + (LATTICE ? lattice_bucket(cx, cy, cz, nb) : (cell_hash(cx, cy, cz) & (nb - 1u)));
                 key[v] = b;
                 act = true;
             }
         }
         const uint32_t m = __ballot_sync(FULL, act);
+        bool first = false;
         if (act) {
             const uint32_t peers = __match_any_sync(m, b);
             const int leader = __ffs(peers) - 1;
@@ -68,16 +94,28 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
             old = __shfl_sync(m, old, leader);
             const uint32_t rank = old + __popc(peers & lanemask_lt());
             arrival[v] = rank;
-            const bool first = rank == 0;
-            const uint32_t fm = __ballot_sync(m, first);
-            if (fm) {
-                const int wl = __ffs(m) - 1;
-                uint32_t base = 0;
-                if ((int)lane == wl) base = atomicAdd(&ctl->occ_count, (uint32_t)__popc(fm));
-                base = __shfl_sync(m, base, wl);
-                if (first) occ[base + __popc(fm & lanemask_lt())] = b;
-            }
+            first = rank == 0;
         }
+        const uint32_t fm = __ballot_sync(FULL, first);
+        if (lane == 0) s_first[it][warp] = __popc(fm);
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            // warp 0: exclusive prefix over the eight warps + one atomic
+            const uint32_t c = lane < 8 ? s_first[it][lane] : 0u;
+            uint32_t inc = c;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, inc, o);
+                if ((int)lane >= o) inc += y;
+            }
+            const uint32_t total = __shfl_sync(FULL, inc, 7);
+            uint32_t base = 0;
+            if (lane == 0 && total) base = atomicAdd(&ctl->occ_count, total);
+            base = __shfl_sync(FULL, base, 0);
+            if (lane < 8) s_first[it][lane] = base + inc - c;
+        }
+        __syncthreads();
+        if (first) occ[s_first[it][warp] + __popc(fm & lanemask_lt())] = b;
     }
 }
 
@@ -234,31 +272,40 @@ __global__ void __launch_bounds__(256) k_alloc(FlockDesc* __restrict__ fl, int n
 // ---------------------------------------------------------------------------
 // pass 3: scatter by arrival rank
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+// Each bird's sort key goes to its slot in its bucket's run: the bird index
+// (the stable order) in the high half, its current view index in the low half.
+__global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
                                                  const uint32_t* __restrict__ key, const uint32_t* __restrict__ arrival,
-                                                 const uint32_t* __restrict__ offsets, uint32_t* __restrict__ tmp,
-                                                 StepCtl* __restrict__ ctl) {
+                                                 const uint32_t* __restrict__ offsets,
+                                                 unsigned long long* __restrict__ tmp, StepCtl* __restrict__ ctl) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
         if (!__ldg(&d->remaining)) continue;
+        const uint32_t bird = ar.id[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
         const uint32_t pos = __ldg(&offsets[key[v]]) + arrival[v];
-        if (pos < V) tmp[pos] = v;
+        if (pos < V) tmp[pos] = ((unsigned long long)bird << 32) | v;
         else atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
     }
 }
 
 // ---------------------------------------------------------------------------
-// pass 4: per-bucket stable order + cell-ordered view + deciding-bird list
+// pass 4: per-bucket stable order; state moves into cell order
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t bitonic32(uint32_t x, uint32_t lane) {
+template <class T>
+__device__ __forceinline__ T kmin(T a, T b) { return a < b ? a : b; }
+template <class T>
+__device__ __forceinline__ T kmax(T a, T b) { return a < b ? b : a; }
+
+template <class T>
+__device__ __forceinline__ T bitonic32(T x, uint32_t lane) {
 #pragma unroll
     for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
-            const uint32_t y = __shfl_xor_sync(FULL, x, j);
+            const T y = __shfl_xor_sync(FULL, x, j);
             const bool up = (lane & k) == 0;
             const bool lower = (lane & j) == 0;
-            x = (lower == up) ? min(x, y) : max(x, y);
+            x = (lower == up) ? kmin(x, y) : kmax(x, y);
         }
     }
     return x;
@@ -266,8 +313,8 @@ __device__ __forceinline__ uint32_t bitonic32(uint32_t x, uint32_t lane) {
 
 // Bitonic sort of 32*R keys held R per lane (element i = lane + 32*k in x[k]),
 // ascending; stages with stride >= 32 swap between a lane's own registers.
-template <int R>
-__device__ __forceinline__ void bitonic_lanes(uint32_t (&x)[R], uint32_t lane) {
+template <int R, class T>
+__device__ __forceinline__ void bitonic_lanes(T (&x)[R], uint32_t lane) {
     constexpr int N = 32 * R;
 #pragma unroll
     for (int s = 2; s <= N; s <<= 1) {
@@ -280,48 +327,53 @@ __device__ __forceinline__ void bitonic_lanes(uint32_t (&x)[R], uint32_t lane) {
                     const int kp = k ^ jr;
                     if (kp > k) {  // x[k] is the lower element of the pair
                         const bool up = ((lane + 32u * k) & (uint32_t)s) == 0;
-                        const uint32_t a = x[k], b = x[kp];
-                        x[k] = up ? min(a, b) : max(a, b);
-                        x[kp] = up ? max(a, b) : min(a, b);
+                        const T a = x[k], b = x[kp];
+                        x[k] = up ? kmin(a, b) : kmax(a, b);
+                        x[kp] = up ? kmax(a, b) : kmin(a, b);
                     }
                 }
             } else {
 #pragma unroll
                 for (int k = 0; k < R; ++k) {
                     const uint32_t i = lane + 32u * k;
-                    const uint32_t y = __shfl_xor_sync(FULL, x[k], j);
+                    const T y = __shfl_xor_sync(FULL, x[k], j);
                     const bool up = (i & (uint32_t)s) == 0;
                     const bool lower = (i & (uint32_t)j) == 0;
-                    x[k] = (lower == up) ? min(x[k], y) : max(x[k], y);
+                    x[k] = (lower == up) ? kmin(x[k], y) : kmax(x[k], y);
                 }
             }
         }
     }
 }
 
-// Writes one bird of the cell-ordered view at sorted slot `pos` and, when it
-// decides this step, its self-contained decide record. Called by all 32 lanes.
-__device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, const FlockDesc& d, float t_now,
-                                            uint32_t lane, const float4* __restrict__ A, const float4* __restrict__ B,
-                                            const float4* __restrict__ C, const float4* __restrict__ D,
-                                            uint32_t* __restrict__ sorted, float4* __restrict__ spos,
-                                            float4* __restrict__ sfwd, DueRec* __restrict__ due,
+// Moves one bird (sort key x = bird << 32 | old view index) to view index
+// `pos` of the reordered buffer, writes its unit heading to the forward view
+// and, when it decides this step, its self-contained decide record. Called by
+// all 32 lanes.
+__device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned long long x, const FlockDesc& d,
+                                            float t_now, uint32_t lane, const Arena& ar, uint32_t oshift,
+                                            uint32_t nshift, float4* __restrict__ sfwd, DueRec* __restrict__ due,
                                             StepCtl* __restrict__ ctl) {
     bool is_due = false;
-    uint32_t local = 0, st = 0;
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t nst = 0;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), c = a;
     f3 fw = mk(0.f, 0.f, 0.f);
     if (has) {
-        local = v - d.vbase;
-        st = d.sbase + local;
-        a = A[st];
-        const float4 b = B[st];
-        const float nd = __ldg(&D[st].x);
-        sorted[pos] = local;
-        spos[pos] = make_float4(a.x, a.y, a.z, __uint_as_float(local));
+        const uint32_t bird = (uint32_t)(x >> 32);
+        const uint32_t ost = (uint32_t)x + oshift;
+        nst = pos + nshift;
+        a = ar.A[ost];
+        const float4 b = ar.B[ost];
+        c = ar.C[ost];
+        const float4 e = ar.D[ost];
+        ar.A[nst] = a;
+        ar.B[nst] = b;
+        ar.C[nst] = c;
+        ar.D[nst] = e;
+        ar.id[nst] = bird;
         fw = forward(xyz(b));
         sfwd[pos] = make_float4(fw.x, fw.y, fw.z, 0.f);
-        is_due = t_now >= nd;
+        is_due = t_now >= e.x;
     }
     const uint32_t dm = __ballot_sync(FULL, is_due);
     if (dm) {
@@ -330,9 +382,9 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, uint32_t v, 
         base = __shfl_sync(FULL, base, 0);
         if (is_due) {
             DueRec r;
-            r.pr = make_float4(a.x, a.y, a.z, __ldg(&C[st].w));
+            r.pr = make_float4(a.x, a.y, a.z, c.w);
             r.fk = make_float4(fw.x, fw.y, fw.z, __uint_as_float(pos));
-            r.fl = make_uint4(st, d.bbase, d.buckets, d.vbase + local);
+            r.fl = make_uint4(nst, d.bbase, d.buckets, nshift);
             due[base + __popc(dm & lanemask_lt())] = r;
         }
     }
@@ -342,11 +394,9 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
                                                  const uint32_t* __restrict__ counts,
-                                                 const uint32_t* __restrict__ tmp, const float4* __restrict__ A,
-                                                 const float4* __restrict__ B, const float4* __restrict__ C,
-                                                 const float4* __restrict__ D, uint32_t* __restrict__ sorted,
-                                                 float4* __restrict__ spos, float4* __restrict__ sfwd,
-                                                 DueRec* __restrict__ due) {
+                                                 const unsigned long long* __restrict__ tmp, Arena ar,
+                                                 float4* __restrict__ sfwd, DueRec* __restrict__ due) {
+    constexpr unsigned long long PAD = ~0ull;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -356,49 +406,53 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
         const int f = find_flock_b(fl, nfl, b);
         const FlockDesc d = fl[f];
         const float t_now = __fadd_rn(d.time, DT);
+        const uint32_t oshift = view_shift(d.sbase, d.vbase, d.parity, ar.cap), nshift = view_shift(d.sbase, d.vbase, d.parity ^ 1u, ar.cap);
         const uint32_t s0 = __ldg(&offsets[b]), L = __ldg(&counts[b]);
-        if (s0 + L > V || s0 + L < s0) {  // never with valid starts; skip rather than read out of range
+        // a run lies inside its flock's view region; never otherwise with valid
+        // starts, and skipping keeps every slot inside the flock's own range
+        if (s0 < d.vbase || s0 + L > d.vbase + d.n || s0 + L < s0 || s0 + L > V) {
             if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
             continue;
         }
         if (L <= 32) {
-            uint32_t x = lane < L ? tmp[s0 + lane] : 0xFFFFFFFFu;
+            unsigned long long x = lane < L ? tmp[s0 + lane] : PAD;
             x = bitonic32(x, lane);
-            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, A, B, C, D, sorted, spos, sfwd, due, ctl);
+            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, due, ctl);
         } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
-            uint32_t x[2];
+            unsigned long long x[2];
 #pragma unroll
-            for (int k = 0; k < 2; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : 0xFFFFFFFFu;
+            for (int k = 0; k < 2; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
             bitonic_lanes<2>(x, lane);
 #pragma unroll
             for (int k = 0; k < 2; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, A, B, C, D, sorted, spos,
-                            sfwd, due, ctl);
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, due,
+                            ctl);
         } else if (L <= 128) {
-            uint32_t x[4];
+            unsigned long long x[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : 0xFFFFFFFFu;
+            for (int k = 0; k < 4; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
             bitonic_lanes<4>(x, lane);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, A, B, C, D, sorted, spos,
-                            sfwd, due, ctl);
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, due,
+                            ctl);
         } else {
-            // long range (dense cell or hash collision): rank by counting
+            // long range (dense cell or hash collision): rank by counting; bird
+            // indices are distinct within a flock, so ranks are distinct
             for (uint32_t c0 = 0; c0 < L; c0 += 32) {
                 const bool has = c0 + lane < L;
-                const uint32_t x = has ? tmp[s0 + c0 + lane] : 0xFFFFFFFFu;
+                const unsigned long long x = has ? tmp[s0 + c0 + lane] : PAD;
+                const uint32_t xb = (uint32_t)(x >> 32);
                 uint32_t rank = 0;
                 for (uint32_t j0 = 0; j0 < L; j0 += 32) {
-                    const uint32_t y = (j0 + lane < L) ? tmp[s0 + j0 + lane] : 0xFFFFFFFFu;
+                    const uint32_t y = (j0 + lane < L) ? (uint32_t)(tmp[s0 + j0 + lane] >> 32) : 0xFFFFFFFFu;
 #pragma unroll 8
-                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
+                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < xb;
                 }
-                emit_sorted(has, s0 + rank, x, d, t_now, lane, A, B, C, D, sorted, spos, sfwd, due, ctl);
+                emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, due, ctl);
             }
         }
     }
 }
-
 
 }  // namespace flk

@@ -9,17 +9,21 @@ namespace flk {
 // ---------------------------------------------------------------------------
 // pass 6: integrate (model.rs:149-176) + end-of-step bookkeeping
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V,
-                                                   float4* __restrict__ A, float4* __restrict__ B,
-                                                   const float4* __restrict__ C, uint32_t* __restrict__ counts,
-                                                   const uint32_t* __restrict__ occ, StepCtl* __restrict__ ctl) {
+// Works on the buffer the sort pass wrote (parity ^ 1); the last block makes
+// that buffer current.
+__global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
+                                                   uint32_t* __restrict__ counts, const uint32_t* __restrict__ occ,
+                                                   StepCtl* __restrict__ ctl) {
     // the histogram's occupied entries go back to zero for the next step
     const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nocc; i += gridDim.x * blockDim.x) counts[occ[i]] = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
         if (!d->remaining) continue;
-        const uint32_t st = d->sbase + (v - d->vbase);
+        float4* __restrict__ A = ar.A;
+        float4* __restrict__ B = ar.B;
+        const float4* __restrict__ C = ar.C;
+        const uint32_t st = v + view_shift(d->sbase, d->vbase, d->parity ^ 1u, ar.cap);
         const float4 a = A[st];
         const float4 b = B[st];
         const float4 c = C[st];
@@ -69,6 +73,7 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
             if (fl[f].remaining) {
                 fl[f].time = __fadd_rn(fl[f].time, DT);
                 fl[f].remaining -= 1;
+                fl[f].parity ^= 1u;
             }
         }
         if (threadIdx.x == 0) {

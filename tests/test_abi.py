@@ -42,7 +42,7 @@ def test_buckets_for_agrees(native, oracle):
 
 def test_bytes_for_grows_with_n(native):
     assert native.bytes_for(1000) < native.bytes_for(100_000) < native.bytes_for(1_000_000)
-    assert native.bytes_for(1_000_000) < 200 * 1_000_000
+    assert native.bytes_for(1_000_000) < 300 * 1_000_000
     assert native.kernels_per_step() == 6
 
 
