@@ -19,6 +19,8 @@ Also on the same line:
              aggregate bird-updates/s, against the same requests served one
              at a time through the plain step;
   cpu_baseline  the brute-force CPU oracle on a bounded sample of the workload.
+  cpu_grid   the reference GPU backend's grid algorithm restated for the CPU
+             (OpenMP, all host cores), full steps of the same workload.
 
 `--impl reference` times the reference's own CPU step (the C restatement of
 its flock-ref oracle; the Rust original cannot be built on this image) on all
@@ -196,6 +198,23 @@ def cpu_sample(words: np.ndarray, budget_s: float, seed: int = 0) -> dict:
             "sample": f"brute-force decide of {m} of the {len(due)} deciding birds (each against all {n}) "
                       f"+ integrate of all {n}; extrapolated to one step ({step_s:.3f} s)",
             "sample_wall_s": round(t_dec + t_int, 3)}
+
+
+def cpu_grid_steps(words: np.ndarray, steps: int) -> dict:
+    """Full steps of the workload with the reference GPU backend's grid
+    algorithm on all host cores (cuda/flock.cu:190-290 restated in the oracle)."""
+    from oracle import pyoracle as o
+
+    n = len(words)
+    threads = o.max_threads()
+    t, w = 0.0, words
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t, w = o.step_grid(w, t)
+    wall = time.perf_counter() - t0
+    return {"value": n * steps / wall, "unit": "bird-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full grid steps of {n} birds (cell walks with the exact cell check, as "
+                      f"cuda/flock.cu's decide), {wall:.2f} s"}
 
 
 def run_reference(args, dist, rank):
@@ -419,6 +438,7 @@ def main():
             out["batched"] = bench_batched(m, args, local)
             out["served"] = bench_served(m, args, local)
             out["cpu_baseline"] = cpu_sample(m.generate(n, args.seed), args.cpu_budget)
+            out["cpu_grid"] = cpu_grid_steps(m.generate(n, args.seed), 2 if n <= 4_000_000 else 1)
         print(json.dumps(out), flush=True)
     barrier(dist)
     if dist is not None:

@@ -630,3 +630,124 @@ int orc_diff(const orc_bird* a, const orc_bird* b, uint32_t n, float pos_tol, fl
     if (allow == 0) return dp <= pos_tol && dv <= vel_tol && nbm == 0;
     return nout <= allow && dp <= outlier_max && dv <= outlier_max && nbm == 0;
 }
+
+/* ---- CPU grid step: the reference GPU backend's algorithm on host cores ----
+ * cuda/flock.cu:190-290 (decide) restated for the CPU: per deciding bird, an
+ * R walk over the cells of [cell(p - r), cell(p + r)] that pass the sphere
+ * test with its +1e-4 slack (flock.cu:85-91), each cell's bucket range with
+ * the exact cell check (flock.cu:219-221), then the same walk for 2R
+ * (centrality). The grid is the stable counting sort above. OpenMP over the
+ * deciding birds and over integrate. Used only as a timed CPU baseline and
+ * checked against orc_step in the tests. */
+static int cell_hits_sphere(const int32_t c[3], v3 p, float r2) {
+    const float lx = (float)c[0] * P_GRID_CELL, ly = (float)c[1] * P_GRID_CELL, lz = (float)c[2] * P_GRID_CELL;
+    const float dx = f_clamp(p.x, lx, lx + P_GRID_CELL) - p.x;
+    const float dy = f_clamp(p.y, ly, ly + P_GRID_CELL) - p.y;
+    const float dz = f_clamp(p.z, lz, lz + P_GRID_CELL) - p.z;
+    return dx * dx + dy * dy + dz * dz <= r2 + 1e-4f;
+}
+
+static orc_decision grid_decide(uint32_t i, const orc_bird* birds, const uint32_t* offsets, const uint32_t* sorted,
+                                uint32_t mask) {
+    const orc_bird* me = &birds[i];
+    const v3 p = pos_of(me);
+    const float r = me->radius;
+    const v3 f_i = forward(vel_of(me));
+    v3 sep = V0V, coh = V0V, align = V0V, csum = V0V;
+    uint32_t n_all = 0, n_star = 0, n_align = 0, n_g = 0;
+    for (int walk = 0; walk < 2; ++walk) {
+        const float rr = walk == 0 ? r : 2.0f * r;
+        const float r2 = walk == 0 ? r * r : 4.0f * r * r;
+        const float lo_p[3] = {p.x - rr, p.y - rr, p.z - rr}, hi_p[3] = {p.x + rr, p.y + rr, p.z + rr};
+        int32_t lo[3], hi[3], c[3], cq[3];
+        orc_cell_of(lo_p, lo);
+        orc_cell_of(hi_p, hi);
+        for (c[2] = lo[2]; c[2] <= hi[2]; ++c[2])
+            for (c[1] = lo[1]; c[1] <= hi[1]; ++c[1])
+                for (c[0] = lo[0]; c[0] <= hi[0]; ++c[0]) {
+                    if (!cell_hits_sphere(c, p, r2)) continue;
+                    const uint32_t b = orc_bucket_of(c, mask);
+                    for (uint32_t s = offsets[b]; s < offsets[b + 1]; ++s) {
+                        const uint32_t j = sorted[s];
+                        if (j == i) continue;
+                        orc_cell_of(birds[j].pos, cq);
+                        if (cq[0] != c[0] || cq[1] != c[1] || cq[2] != c[2]) continue;
+                        const v3 d = v_sub(pos_of(&birds[j]), p);
+                        const float d2 = v_dot(d, d);
+                        if (d2 > r2) continue;
+                        const float dist = sqrtf(d2);
+                        const v3 dhat = v_div(d, f_max(dist, 1e-6f));
+                        if (walk == 1) {
+                            csum = v_add(csum, dhat);
+                            n_g += 1;
+                            continue;
+                        }
+                        n_all += 1;
+                        float g = 1.0f;
+                        if (dist > P_R_H) {
+                            const float t = dist - P_R_H;
+                            g = expf(-(t * t) / (2.0f * P_SIGMA * P_SIGMA));
+                        }
+                        sep = v_sub(sep, v_mul(dhat, g));
+                        if (dist > P_R_H) {
+                            coh = v_add(coh, dhat);
+                            n_star += 1;
+                        }
+                        if (v_dot(f_i, dhat) >= P_BLIND_COS) {
+                            align = v_add(align, forward(vel_of(&birds[j])));
+                            n_align += 1;
+                        }
+                    }
+                }
+    }
+    v3 force = V0V;
+    if (n_all > 0) force = v_add(force, v_mul(sep, P_W_SEP / (float)n_all));
+    const float centrality = n_g > 0 ? v_len(csum) / (float)n_g : 0.0f;
+    if (n_star > 0) force = v_add(force, v_mul(v_normalize_or_zero(coh), P_W_COH * centrality));
+    const v3 a = n_align > 0 ? v_sub(v_div(align, (float)n_align), f_i) : V0V;
+    force = v_add(force, v_mul(a, P_W_ALIGN));
+    force = v_add(force, v_mul(VZ, P_W_ROOST_V * f_clamp((P_Z0 - p.z) / P_H_ROOST_V, -1.0f, 1.0f)));
+    const float speed = v_len(vel_of(me));
+    force = v_add(force, v_mul(f_i, (P_MASS / P_TAU) * (P_V0 - speed)));
+    orc_decision out;
+    out.force[0] = force.x; out.force[1] = force.y; out.force[2] = force.z;
+    out.radius = orc_radius_step(r, n_all);
+    out.neighbours = n_all;
+    out.centrality = centrality;
+    return out;
+}
+
+float orc_step_grid(orc_bird* birds, uint32_t n, float time, int threads) {
+    time += P_DT;
+    const uint32_t buckets = orc_buckets_for(n);
+    uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    uint32_t* offsets = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)buckets + 1));
+    uint32_t* sorted = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    orc_decision* dec = (orc_decision*)malloc(sizeof(orc_decision) * (n ? n : 1));
+    orc_grid(birds, n, buckets, keys, offsets, sorted);
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+#endif
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+        const uint32_t i = (uint32_t)ii;
+        if (time >= birds[i].next_decision) dec[i] = grid_decide(i, birds, offsets, sorted, buckets - 1u);
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!(time >= birds[i].next_decision)) continue;
+        birds[i].steer[0] = dec[i].force[0];
+        birds[i].steer[1] = dec[i].force[1];
+        birds[i].steer[2] = dec[i].force[2];
+        birds[i].radius = dec[i].radius;
+        birds[i].neighbours = dec[i].neighbours;
+        birds[i].centrality = dec[i].centrality;
+        birds[i].next_decision += P_DU;
+    }
+    orc_integrate_all(birds, n, threads);
+    free(keys);
+    free(offsets);
+    free(sorted);
+    free(dec);
+    (void)threads;
+    return time;
+}

@@ -18,6 +18,7 @@
  *   stats/statdiff/diff  crates/flock-ref/src/main.rs:83-208
  *   grid keys / buckets  cuda/flock.cu:75-83, 368-372
  *   grid invariants      cutile/src/main.rs:307-362 (check_grid)
+ *   CPU grid step        cuda/flock.cu:85-91, 190-290 (orc_step_grid, a baseline)
  *
  * Vector arithmetic follows glam 0.34.1's scalar Vec3 (the reference's
  * Cargo.lock:219-221; glam is not vendored): component-wise f32 operations,
@@ -114,6 +115,11 @@ void orc_integrate_all(orc_bird* birds, uint32_t n, int threads);
 
 /* Grid restatement (cuda/flock.cu:75-83, 368-372) with the canonical stable
  * order (bucket, then bird index). keys: n, offsets: buckets+1, sorted: n. */
+/* One step with the reference GPU backend's grid algorithm (cuda/flock.cu:
+ * 190-290: R and 2R cell walks with the exact cell check) run on host cores;
+ * a CPU baseline, checked against orc_step. Returns the new time. */
+float orc_step_grid(orc_bird* birds, uint32_t n, float time, int threads);
+
 uint32_t orc_buckets_for(uint32_t n);
 void orc_cell_of(const float p[3], int32_t c[3]);
 uint32_t orc_bucket_of(const int32_t c[3], uint32_t mask);

@@ -51,6 +51,7 @@ def lib() -> C.CDLL:
             "orc_step_f64": (C.c_double, [_PF, C.c_uint32, C.c_float, _PD, C.c_int]),
             "orc_decide_sample": (C.c_double, [_PF, C.c_uint32, _PU, C.c_uint32, C.c_int]),
             "orc_integrate_all": (None, [_PF, C.c_uint32, C.c_int]),
+            "orc_step_grid": (C.c_float, [_PF, C.c_uint32, C.c_float, C.c_int]),
             "orc_decide_many": (None, [_PF, C.c_uint32, _PU, C.c_uint32, _PU, _PF, C.c_int]),
             "orc_buckets_for": (C.c_uint32, [C.c_uint32]),
             "orc_grid": (None, [_PF, C.c_uint32, C.c_uint32, _PU, _PU, _PU]),
@@ -155,6 +156,14 @@ def integrate_all(words: np.ndarray, threads: int = 0) -> np.ndarray:
     w = _w(words).copy()
     lib().orc_integrate_all(_f(w), w.shape[0], threads)
     return w
+
+
+def step_grid(words: np.ndarray, time: float, threads: int = 0):
+    """One step with the reference GPU backend's grid algorithm on host cores
+    (cuda/flock.cu:190-290): the CPU grid baseline. Returns (time, words)."""
+    w = _w(words).copy()
+    t = lib().orc_step_grid(_f(w), w.shape[0], time, threads)
+    return t, w
 
 
 def buckets_for(n: int) -> int:

@@ -180,3 +180,20 @@ def test_radius_step_matches_params_rs(oracle):
     assert oracle.radius_step(0.1, 10_000) == np.float32(0.2)
     r = oracle.radius_step(1.5, 6)
     assert 1.5 < r < 1.51
+
+
+def test_cpu_grid_step_matches_the_brute_force_oracle(oracle):
+    # The CPU grid baseline (the reference GPU backend's cell walks on host
+    # cores) decides like the brute-force oracle: same neighbour counts, radii
+    # and next decisions; sums in another order agree to rounding.
+    for n, seed, k in [(2000, 1, 3), (20_000, 4, 1)]:
+        w = oracle.scatter(n, seed)
+        tg, g = 0.0, w
+        tc, c = 0.0, w
+        for _ in range(k):
+            tg, g = oracle.step_grid(g, tg)
+            tc, c, _, _ = oracle.step(c, tc, with_sets=False)
+        assert np.float32(tg) == np.float32(tc)
+        ok, maxes, mism, _ = oracle.diff(g, c)
+        assert ok and mism == 0, maxes
+        assert np.array_equal(g[:, 8], c[:, 8]) and np.array_equal(g[:, 12], c[:, 12])
