@@ -135,6 +135,22 @@ int flk_pool_create(int32_t device, uint64_t budget_bytes, uint32_t chunk_steps,
  * `out_time`, which may alias the input. */
 int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float* words, uint32_t steps, float* out_words,
                     float* out_time, uint64_t* ticket);
+/* flk_pool_submit with the state read from a .flk file (state.rs:104-171);
+ * the pool holds its own copy of the input. The result buffer must hold
+ * `out_capacity` birds; *n_out receives the flock's size (flk_file_info reads
+ * it beforehand). No counterpart in the reference, whose tools read a file
+ * per process (cuda/flock.cu:340-354). */
+int flk_pool_submit_file(flk_pool* p, const char* path, uint32_t steps, float* out_words, uint32_t out_capacity,
+                         float* out_time, uint64_t* ticket, uint32_t* n_out);
+/* Copies a request's current state into `words` (n*15 words) without pausing
+ * the other flocks: a queued request gives its input (0 steps done), a
+ * resident one its state at the next chunk boundary (packed on the compute
+ * stream, copied on the copy stream while the next chunk runs), a finished
+ * one its result. Blocks until the copy has landed. With `path`, also writes
+ * the state as a .flk file, so submitting that file with the remaining steps
+ * continues the flock exactly. No counterpart in the reference. */
+int flk_pool_snapshot(flk_pool* p, uint64_t ticket, float* words, float* time, uint32_t* steps_done,
+                      const char* path);
 /* *state: 0 queued, 1 resident, 2 done, negative FLK_ERR_* on failure. */
 int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state);
 /* Blocks until done; *latency_ms = completion - submission (host clock). */
@@ -144,6 +160,8 @@ void flk_pool_destroy(flk_pool* p);
 
 /* ---- helpers -------------------------------------------------------------- */
 const char* flk_last_error(void);
+/* Bird count and clock from a .flk header (state.rs:104-171). */
+int flk_file_info(const char* path, uint32_t* n, float* time);
 /* Canonical bucket count: next power of two >= 2n clamped to [2^16, 2^22]. */
 uint32_t flk_buckets_for(uint32_t n);
 /* The benchmark scatter (state.rs:79-101): n birds, SplitMix64 seed. */

@@ -91,12 +91,15 @@ _SIGS = {
     "flk_batch_destroy": (None, [_P]),
     "flk_pool_create": (C.c_int, [C.c_int32, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
     "flk_pool_submit": (C.c_int, [_P, C.c_uint32, C.c_float, _PF, C.c_uint32, _PF, _PF, _PU64]),
+    "flk_pool_submit_file": (C.c_int, [_P, C.c_char_p, C.c_uint32, _PF, C.c_uint32, _PF, _PU64, _PU]),
+    "flk_pool_snapshot": (C.c_int, [_P, C.c_uint64, _PF, _PF, _PU, C.c_char_p]),
     "flk_pool_poll": (C.c_int, [_P, C.c_uint64, _PI]),
     "flk_pool_wait": (C.c_int, [_P, C.c_uint64, _PD]),
     "flk_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
     "flk_pool_destroy": (None, [_P]),
     "flk_last_error": (C.c_char_p, []),
     "flk_buckets_for": (C.c_uint32, [C.c_uint32]),
+    "flk_file_info": (C.c_int, [C.c_char_p, _PU, _PF]),
     "flk_generate": (C.c_int, [C.c_uint32, C.c_uint64, _PF]),
     "flk_params": (C.c_int, [_PF, C.c_int32]),
     "flk_bytes_for": (C.c_uint64, [C.c_uint32]),
@@ -176,6 +179,14 @@ def generate(n: int, seed: int = 1) -> np.ndarray:
     w = np.zeros((n, WORDS), dtype=np.float32)
     _check(lib().flk_generate(n, seed, _fptr(w)))
     return w
+
+
+def file_info(path: str) -> tuple[int, float]:
+    """(birds, time) from a .flk header, read by the library."""
+    n = C.c_uint32()
+    t = C.c_float()
+    _check(lib().flk_file_info(path.encode(), C.byref(n), C.byref(t)))
+    return n.value, t.value
 
 
 def buckets_for(n: int) -> int:
@@ -403,6 +414,31 @@ class Pool:
                                      C.byref(tk)))
         self._keep[tk.value] = (w, o, t)  # buffers must outlive the request
         return tk.value
+
+    def submit_file(self, path: str, steps: int) -> int:
+        """simulate(flock, steps) for the state in a .flk file (the pool keeps its own copy)."""
+        n, _ = file_info(path)
+        o = np.empty((n, WORDS), dtype=np.float32)
+        t = np.zeros(1, dtype=np.float32)
+        tk = C.c_uint64()
+        got = C.c_uint32()
+        _check(lib().flk_pool_submit_file(self._h, path.encode(), steps, _fptr(o), n, _fptr(t), C.byref(tk),
+                                          C.byref(got)))
+        self._keep[tk.value] = (None, o, t)
+        return tk.value
+
+    def snapshot(self, ticket: int, path: Optional[str] = None) -> tuple[float, np.ndarray, int]:
+        """The request's current state without pausing the other flocks:
+        (time, words, steps done); with `path`, also written as a .flk file."""
+        if ticket not in self._keep:
+            raise ValueError("snapshot: unknown ticket, or its result was already collected by wait()")
+        o = self._keep[ticket][1]
+        w = np.empty_like(o)
+        t = np.zeros(1, dtype=np.float32)
+        k = C.c_uint32()
+        _check(lib().flk_pool_snapshot(self._h, ticket, _fptr(w), _fptr(t), C.byref(k),
+                                       path.encode() if path else None))
+        return float(t[0]), w, k.value
 
     def poll(self, ticket: int) -> int:
         s = C.c_int32()

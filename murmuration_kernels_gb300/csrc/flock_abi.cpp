@@ -410,6 +410,17 @@ struct Request {
     Clock::time_point t_submit, t_done;
     int state = 0;  // 0 queued, 1 resident, 2 done, <0 error
     int flock = -1;
+    float result_time = 0.f;
+    std::vector<float> owned;  // the input state, when the pool holds its own copy (file restore)
+};
+
+// A copy of a resident flock's state taken at a chunk boundary.
+struct Snapshot {
+    std::shared_ptr<Request> r;
+    float* words;
+    float time = 0.f;
+    uint32_t steps_done = 0;
+    int state = 0;  // 0 pending, 1 landed, <0 error
 };
 }  // namespace
 
@@ -418,6 +429,7 @@ struct Retire {
     cudaEvent_t done;  // recorded when the result has reached the caller's buffer
     float time;
     bool failed;
+    std::shared_ptr<Snapshot> snap;  // set: this copy is a snapshot, not the request's result
 };
 
 struct flk_pool {
@@ -430,6 +442,7 @@ struct flk_pool {
     std::map<uint64_t, std::shared_ptr<Request>> reqs;
     std::vector<std::shared_ptr<Request>> resident;  // admitted, in flight
     std::deque<Retire> retiring;                     // results on their way to the host
+    std::vector<std::shared_ptr<Snapshot>> snaps;    // snapshots of resident flocks, waiting for a boundary
     uint64_t next_ticket = 1;
     uint64_t resident_bytes = 0;
     bool stop = false, stop_completer = false;
@@ -495,6 +508,25 @@ void flk_pool::loop() {
                 for (auto& r : live) ids.push_back(r->flock);
                 const std::vector<uint32_t> left = eng->remaining_of(ids);
                 std::vector<Retire> done;
+                // snapshots: packed now, on the compute stream, copied out while the next chunk runs
+                std::vector<std::shared_ptr<Snapshot>> snap_now;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    snap_now.swap(snaps);
+                }
+                for (auto& sn : snap_now) {
+                    const auto it = std::find(live.begin(), live.end(), sn->r);
+                    Retire x{sn->r, nullptr, 0.f, err != 0, sn};
+                    FLK_CUDA_ABI(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+                    if (it == live.end() || err) {  // never for a resident request; fail rather than wait
+                        x.failed = true;
+                        FLK_CUDA_ABI(cudaEventRecord(x.done, eng->stream()));
+                    } else {
+                        sn->steps_done = sn->r->steps - left[it - live.begin()];
+                        eng->read_flock_async(sn->r->flock, &sn->time, sn->words, x.done);
+                    }
+                    done.push_back(x);
+                }
                 for (size_t k = 0; k < live.size(); ++k) {
                     if (left[k] != 0 && !err) continue;
                     Retire x{live[k], nullptr, 0.f, err != 0};
@@ -509,8 +541,10 @@ void flk_pool::loop() {
                 stats.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
                 stats.chunks += 1;
                 for (auto& x : done) {
-                    resident_bytes -= x.r->bytes;  // the slot is reusable in stream order
-                    resident.erase(std::find(resident.begin(), resident.end(), x.r));
+                    if (!x.snap) {
+                        resident_bytes -= x.r->bytes;  // the slot is reusable in stream order
+                        resident.erase(std::find(resident.begin(), resident.end(), x.r));
+                    }
                     retiring.push_back(x);
                 }
                 stats.resident_bytes = resident_bytes;
@@ -552,7 +586,13 @@ void flk_pool::complete_loop() {
         cudaEventDestroy(x.done);
         std::lock_guard<std::mutex> lk(mu);
         retiring.pop_front();
+        if (x.snap) {
+            x.snap->state = (x.failed || e != cudaSuccess) ? FLK_ERR_DEVICE : 1;
+            cv_done.notify_all();
+            continue;
+        }
         x.r->t_done = Clock::now();
+        x.r->result_time = x.time;
         if (x.r->out_time) *x.r->out_time = x.time;
         if (x.failed || e != cudaSuccess) {
             x.r->state = x.failed ? FLK_ERR_DEVICE : FLK_ERR_CUDA;
@@ -584,10 +624,13 @@ extern "C" int flk_pool_create(int32_t device, uint64_t budget_bytes, uint32_t c
     });
 }
 
-extern "C" int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float* words, uint32_t steps,
-                               float* out_words, float* out_time, uint64_t* ticket) {
-    if (!p || !ticket || (n && (!words || !out_words))) return fail(FLK_ERR_ARG, "flk_pool_submit: null pointer");
+static int pool_submit(flk_pool* p, uint32_t n, float time, const float* words, std::vector<float>* owned,
+                       uint32_t steps, float* out_words, float* out_time, uint64_t* ticket) {
     auto r = std::make_shared<Request>();
+    if (owned) {
+        r->owned.swap(*owned);
+        words = r->owned.data();
+    }
     r->n = n;
     r->steps = steps;
     r->time = time;
@@ -607,6 +650,7 @@ extern "C" int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float*
     if (steps == 0) {  // nothing to simulate: complete immediately with the input state
         if (n && out_words != words) std::memcpy(out_words, words, (size_t)n * flk::WORDS * 4);
         if (out_time) *out_time = time;
+        r->result_time = time;
         r->state = 2;
         r->t_done = r->t_submit;
         p->stats.completed += 1;
@@ -619,6 +663,66 @@ extern "C" int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float*
     *ticket = r->ticket;
     p->cv_work.notify_one();
     return FLK_OK;
+}
+
+extern "C" int flk_pool_submit(flk_pool* p, uint32_t n, float time, const float* words, uint32_t steps,
+                               float* out_words, float* out_time, uint64_t* ticket) {
+    if (!p || !ticket || (n && (!words || !out_words))) return fail(FLK_ERR_ARG, "flk_pool_submit: null pointer");
+    return pool_submit(p, n, time, words, nullptr, steps, out_words, out_time, ticket);
+}
+
+extern "C" int flk_pool_submit_file(flk_pool* p, const char* path, uint32_t steps, float* out_words,
+                                    uint32_t out_capacity, float* out_time, uint64_t* ticket, uint32_t* n_out) {
+    if (!p || !path || !ticket) return fail(FLK_ERR_ARG, "flk_pool_submit_file: null pointer");
+    float time = 0.f;
+    std::vector<float> w;
+    const int rc = read_flk(path, &time, &w);
+    if (rc != FLK_OK) return rc;
+    const uint32_t n = (uint32_t)(w.size() / flk::WORDS);
+    if (n_out) *n_out = n;
+    if (n > out_capacity) return fail(FLK_ERR_CAPACITY, "flk_pool_submit_file: " + std::to_string(n) +
+                                                           " birds do not fit the result buffer");
+    if (n && !out_words) return fail(FLK_ERR_ARG, "flk_pool_submit_file: null result buffer");
+    return pool_submit(p, n, time, w.data(), &w, steps, out_words, out_time, ticket);
+}
+
+extern "C" int flk_pool_snapshot(flk_pool* p, uint64_t ticket, float* words, float* time, uint32_t* steps_done,
+                                 const char* path) {
+    if (!p) return fail(FLK_ERR_ARG, "flk_pool_snapshot: null handle");
+    std::unique_lock<std::mutex> lk(p->mu);
+    auto it = p->reqs.find(ticket);
+    if (it == p->reqs.end()) return fail(FLK_ERR_ID, "flk_pool_snapshot: unknown ticket");
+    auto r = it->second;
+    if (r->n && !words) return fail(FLK_ERR_ARG, "flk_pool_snapshot: null words");
+    if (r->state == 1 && std::find(p->resident.begin(), p->resident.end(), r) == p->resident.end())
+        p->cv_done.wait(lk, [&] { return r->state != 1 || p->stop; });  // retiring: its result is landing
+    if (r->state < 0) return fail(r->state, "flk_pool_snapshot: request failed: " + p->worker_error);
+    if (r->state == 1 && p->stop) return fail(FLK_ERR_CUDA, "flk_pool_snapshot: pool stopped");
+    float t = 0.f;
+    uint32_t k = 0;
+    const size_t bytes = (size_t)r->n * flk::WORDS * 4;
+    if (r->state == 0) {  // still queued: its input state
+        if (bytes) std::memcpy(words, r->words, bytes);
+        t = r->time;
+    } else if (r->state == 2) {  // finished: its result
+        if (bytes) std::memcpy(words, r->out_words, bytes);
+        t = r->result_time;
+        k = r->steps;
+    } else {  // resident: taken at the next chunk boundary while the others keep running
+        auto sn = std::make_shared<Snapshot>();
+        sn->r = r;
+        sn->words = words;
+        p->snaps.push_back(sn);
+        p->cv_work.notify_one();
+        p->cv_done.wait(lk, [&] { return sn->state != 0 || p->stop; });
+        if (sn->state != 1) return fail(sn->state ? sn->state : FLK_ERR_CUDA, "flk_pool_snapshot: copy failed");
+        t = sn->time;
+        k = sn->steps_done;
+    }
+    lk.unlock();
+    if (time) *time = t;
+    if (steps_done) *steps_done = k;
+    return path ? write_flk(path, t, words, r->n) : FLK_OK;
 }
 
 extern "C" int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state) {
@@ -676,6 +780,21 @@ extern "C" void flk_pool_destroy(flk_pool* p) {
 extern "C" const char* flk_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" uint32_t flk_buckets_for(uint32_t n) { return flk::buckets_for(n); }
+
+extern "C" int flk_file_info(const char* path, uint32_t* n, float* time) {
+    if (!path) return fail(FLK_ERR_ARG, "flk_file_info: null path");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(FLK_ERR_IO, std::string(path) + ": cannot open");
+    uint32_t head[4];
+    const bool got = std::fread(head, 4, 4, fp) == 4;
+    std::fclose(fp);
+    if (!got) return fail(FLK_ERR_IO, std::string(path) + ": truncated header");
+    if (std::memcmp(head, "FLK1", 4) != 0 || head[2] != (uint32_t)flk::WORDS)
+        return fail(FLK_ERR_FORMAT, std::string(path) + ": not a FLK1 file with 15 words per bird");
+    if (n) *n = head[1];
+    if (time) std::memcpy(time, &head[3], 4);
+    return FLK_OK;
+}
 
 // SplitMix64 scatter (reference crates/flock-ref/src/state.rs:58-101): per
 // bird, 3 position draws, 3 jitter draws, 1 decision-phase draw.

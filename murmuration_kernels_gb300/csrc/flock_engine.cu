@@ -94,6 +94,7 @@ Engine::Engine(int device) {
     radius_table_ = dalloc<float>(RADIUS_TABLE, &dev_bytes_);
     FLK_CUDA(cudaMemcpyAsync(radius_table_, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, stream_));
     FLK_CUDA(cudaStreamSynchronize(stream_));
+    set_shape(shape_);  // decide's shared memory may exceed the default 48 KB per CTA
 }
 
 Engine::~Engine() {

@@ -95,3 +95,18 @@ def test_python_flk_helpers_match_the_oracle_writer(native, oracle, tmp_path):
         bad = tmp_path / "x.flk"
         bad.write_bytes(b"nope")
         native.read_flk(str(bad))
+
+
+def test_file_info_reads_the_header(native, tmp_path):
+    w = native.generate(123, 5)
+    path = str(tmp_path / "x.flk")
+    native.write_flk(path, 0.375, w)
+    assert native.file_info(path) == (123, 0.375)
+    with pytest.raises(native.FlockError) as e:
+        native.file_info(str(tmp_path / "missing.flk"))
+    assert e.value.code == -2
+    bad = tmp_path / "bad.flk"
+    bad.write_bytes(b"FLK2" + bytes(12))
+    with pytest.raises(native.FlockError) as e:
+        native.file_info(str(bad))
+    assert e.value.code == -7

@@ -454,3 +454,92 @@ def test_pool_rejects_a_request_over_budget(native):
         assert e.value.code == -8
         t = pool.submit(native.generate(800, 1), 0)  # zero steps completes at once
         assert pool.wait(t)[0] == 0.0
+
+
+def test_parity_ladder_batched_and_served(native, oracle):
+    """The reference's ladder (scripts/parity.sh: K = 1, 10, 30 strict; 100
+    with <= 2 outliers <= 1e-2; 1000 aggregate statdiff) per flock of a batch,
+    and per request of the serving pool."""
+    sizes = [2000, 700, 3000]
+    flocks = [oracle.scatter(n, 50 + k) for k, n in enumerate(sizes)]
+    b = native.Batch()
+    ids = [b.add(w) for w in flocks]
+    cpu = [(0.0, w) for w in flocks]
+    done = 0
+    for k in (1, 10, 30, 100, 1000):
+        b.step(k - done)
+        cpu = [oracle.steps(c, t, k - done) for t, c in cpu]
+        done = k
+        for fid, (t_cpu, c) in zip(ids, cpu):
+            t_gpu, g = b.read(fid)
+            assert t_gpu == np.float32(t_cpu)
+            if k <= 30:
+                ok, maxes, mism, _ = oracle.diff(g, c)
+                assert ok, (k, len(c), maxes, mism)
+            elif k <= 100:
+                ok, maxes, mism, outl = oracle.diff(g, c, allow=2, outlier_max=1e-2)
+                assert ok, (k, len(c), maxes, mism, outl)
+            else:
+                ok, d = oracle.statdiff(g, c)
+                assert ok, (k, len(c), d)
+    b.close()
+    # served: one request per rung, all in flight together
+    w0 = oracle.scatter(1500, 60)
+    rungs = (1, 10, 30, 100)
+    with native.Pool(budget_bytes=native.bytes_for(50_000), chunk_steps=7) as pool:
+        tickets = [pool.submit(w0, k) for k in rungs]
+        results = [pool.wait(t) for t in tickets]
+    for k, (t_gpu, g, _) in zip(rungs, results):
+        t_cpu, c = oracle.steps(w0, 0.0, k)
+        assert t_gpu == np.float32(t_cpu)
+        if k <= 30:
+            ok, maxes, mism, _ = oracle.diff(g, c)
+        else:
+            ok, maxes, mism, _ = oracle.diff(g, c, allow=2, outlier_max=1e-2)
+        assert ok, (k, maxes, mism)
+
+
+def test_pool_snapshot_and_restore_continue_exactly(native, tmp_path):
+    """A snapshot of a resident flock, taken while the others keep running,
+    equals the plain step after the reported number of steps; submitting the
+    snapshot file for the remaining steps ends exactly where the original
+    request ends. Queued and finished requests snapshot as their input and
+    their result."""
+    a = native.generate(5000, 71)
+    others = [native.generate(3000, 72), native.generate(8000, 73)]
+    path = str(tmp_path / "snap.flk")
+    with native.Pool(budget_bytes=native.bytes_for(20_000), chunk_steps=4) as pool:
+        ta = pool.submit(a, 60)
+        tos = [pool.submit(w, s) for w, s in zip(others, (40, 80))]
+        while pool.poll(ta) == 0:
+            pass
+        t_s, w_s, k = pool.snapshot(ta, path)
+        assert 0 <= k <= 60
+        rest = pool.submit_file(path, 60 - k)
+        t1, w1, _ = pool.wait(ta)
+        t2, w2, _ = pool.wait(rest)
+        for t in tos:
+            pool.wait(t)
+    assert t1 == t2 and w1.tobytes() == w2.tobytes()
+    p = native.Flock(a)
+    p.step(k)
+    tp, wp = p.read()
+    p.close()
+    assert tp == t_s and wp.tobytes() == w_s.tobytes()
+    n, t_file = native.file_info(path)
+    assert n == 5000 and t_file == t_s
+    assert native.read_flk(path)[1].tobytes() == w_s.tobytes()
+    # a queued request (the budget holds one flock) and a finished one
+    big = native.generate(9000, 74)
+    with native.Pool(budget_bytes=native.bytes_for(9000), chunk_steps=3) as pool:
+        t_run = pool.submit(big, 2000)  # long enough that the second request is still queued below
+        t_wait = pool.submit(big, 5, time=0.25)
+        assert pool.poll(t_wait) == 0
+        tq, wq, kq = pool.snapshot(t_wait)
+        assert kq == 0 and tq == np.float32(0.25) and wq.tobytes() == big.tobytes()
+        while pool.poll(t_run) != 2:
+            pass
+        tf, wf, kf = pool.snapshot(t_run)
+        t_end, w_end, _ = pool.wait(t_run)
+        assert kf == 2000 and tf == t_end and wf.tobytes() == w_end.tobytes()
+        pool.wait(t_wait)
