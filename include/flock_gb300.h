@@ -80,6 +80,14 @@ int flk_size(const flk_flock* f, uint32_t* n, uint32_t* buckets);
 int flk_step_debug(flk_flock* f, uint32_t* keys, uint32_t* offsets, uint32_t* sorted, uint32_t* sets);
 /* Cumulative deciding birds, candidate tests and pairs within 2R. */
 int flk_counters(flk_flock* f, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
+/* One step (exactly flk_step(f, 1)) that also evaluates the same step in FP64
+ * from the same input state, for error reports on a live flock. `out64`
+ * (optional, n*15 doubles, bird order) receives the FP64 post-step state;
+ * `report` (optional, 4 doubles) the f32 step's maximum relative position
+ * error, maximum relative velocity error, neighbour-count mismatches and the
+ * number of deciding birds. The reference evaluates only in f32; its oracle
+ * (crates/flock-ref/src/model.rs:53-176) is what the FP64 pass restates. */
+int flk_step_f64(flk_flock* f, double* out64, double* report);
 /* Measurement helper (no counterpart in the reference, whose main() times
  * passes inline, cuda/flock.cu:447-492): runs `steps` steps one graph launch
  * at a time; before each step it overwrites a `flush_bytes` device buffer so

@@ -75,6 +75,7 @@ _SIGS = {
     "flk_size": (C.c_int, [_P, _PU, _PU]),
     "flk_step_debug": (C.c_int, [_P, _PU, _PU, _PU, _PU]),
     "flk_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
+    "flk_step_f64": (C.c_int, [_P, _PD, _PD]),
     "flk_time_steps": (C.c_int, [_P, C.c_uint32, C.c_uint64, _PF]),
     "flk_close": (None, [_P]),
     "flk_batch_create": (C.c_int, [C.c_int32, C.POINTER(_P)]),
@@ -277,6 +278,15 @@ class Flock:
         sets = np.zeros((self.n, 8), dtype=np.uint32)
         _check(lib().flk_step_debug(self._h, _uptr(keys), _uptr(offs), _uptr(srt), _uptr(sets)))
         return {"keys": keys, "offsets": offs, "sorted": srt, "sets": sets}
+
+    def step_f64(self) -> tuple[np.ndarray, dict[str, float]]:
+        """One step (as step(1)) that also evaluates it in FP64 from the same
+        state: (FP64 post-step state [n, 15], error report of the f32 step)."""
+        out = np.empty((self.n, WORDS), dtype=np.float64)
+        rep = np.zeros(4, dtype=np.float64)
+        _check(lib().flk_step_f64(self._h, out.ctypes.data_as(_PD), rep.ctypes.data_as(_PD)))
+        return out, {"max_rel_pos": float(rep[0]), "max_rel_vel": float(rep[1]),
+                     "neighbour_mismatches": int(rep[2]), "deciding": int(rep[3])}
 
     def counters(self) -> tuple[int, int, int]:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()

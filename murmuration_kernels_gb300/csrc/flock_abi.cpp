@@ -197,6 +197,20 @@ extern "C" int flk_step_debug(flk_flock* f, uint32_t* keys, uint32_t* offsets, u
     });
 }
 
+extern "C" int flk_step_f64(flk_flock* f, double* out64, double* report) {
+    if (!f) return fail(FLK_ERR_ARG, "flk_step_f64: null handle");
+    return guarded([&] {
+        f->eng->set_remaining({f->id}, {1u});
+        std::vector<std::vector<double>> out;
+        double rep[4];
+        f->eng->step_f64(&out, rep);
+        if (out.size() != 1) return fail(FLK_ERR_ARG, "flk_step_f64: flock not stepped");
+        if (out64 && !out[0].empty()) std::memcpy(out64, out[0].data(), out[0].size() * 8);
+        if (report) std::memcpy(report, rep, sizeof rep);
+        return check_device(*f->eng);
+    });
+}
+
 extern "C" int flk_counters(flk_flock* f, uint64_t* due, uint64_t* cand, uint64_t* pairs) {
     if (!f) return fail(FLK_ERR_ARG, "flk_counters: null handle");
     return guarded([&] {

@@ -39,6 +39,7 @@
 #include "flock_engine.h"
 #include "flock_params.h"
 #include "k_decide.cuh"
+#include "k_fp64.cuh"
 #include "k_grid.cuh"
 #include "k_integrate.cuh"
 
@@ -107,6 +108,7 @@ Engine::~Engine() {
     dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
     dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
+    dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_); dfree(ndue64_);
     if (copy_) cudaStreamDestroy(copy_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -571,7 +573,7 @@ static int pgrid(int sms, int per_sm, uint64_t items, uint64_t per_cta) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * per_sm, need));
 }
 
-void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
+void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64) {
     device_ahead_ = true;
     const int nfl = (int)table_h_.size();
     const int sblocks = pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256);
@@ -594,6 +596,11 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
     k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
         table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, ar_, sfwd_, due_);
+    if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
+        k_decide_f64<<<pgrid(num_sms_, 8, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
+                                                                      counts_, ar_, dec64_, ndue64_);
+        k_integrate_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
+    }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
     // per-warp hit queue + reduced birds awaiting their epilogue
@@ -607,6 +614,7 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev) {
                                                                         counts_, ar_, sfwd_, radius_table_, nullptr);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
     k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, counts_, occ_, ctl_);
+    if (f64) k_compare_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
 }
 
@@ -731,6 +739,71 @@ void Engine::step_debug(std::vector<GridDebug>* out) {
     }
     sync_times();  // clocks and countdowns from the device table
     table_dirty_ = true;
+}
+
+void Engine::step_f64(std::vector<std::vector<double>>* out, double report[4]) {
+    FLK_CUDA(cudaSetDevice(device_));
+    prepare(false);  // production buckets: the FP64 passes use the lattice index
+    out->clear();
+    for (int k = 0; k < 4; ++k) report[k] = 0.0;
+    if (table_h_.empty()) return;
+    if (V_ > f64_V_ || !dec64_) {
+        dfree(dec64_);
+        dfree(out64_);
+        dec64_ = dalloc<double>((size_t)V_ * 8, &dev_bytes_);
+        out64_ = dalloc<double>((size_t)V_ * 15, &dev_bytes_);
+        f64_V_ = V_;
+    }
+    if (table_h_.size() > active_cap_ || !active_) {
+        dfree(active_);
+        active_cap_ = (uint32_t)table_h_.size();
+        active_ = dalloc<uint8_t>(active_cap_, &dev_bytes_);
+    }
+    if (!err64_) err64_ = dalloc<uint32_t>(4, &dev_bytes_);
+    if (!ndue64_) ndue64_ = dalloc<unsigned long long>(1, &dev_bytes_);
+    const std::vector<FlockDesc> before = table_h_;
+    std::vector<uint8_t> act(before.size());
+    for (size_t k = 0; k < before.size(); ++k) act[k] = before[k].remaining > 0;
+    FLK_CUDA(cudaMemcpyAsync(active_, act.data(), act.size(), cudaMemcpyHostToDevice, stream_));
+    FLK_CUDA(cudaMemsetAsync(err64_, 0, 16, stream_));
+    FLK_CUDA(cudaMemsetAsync(ndue64_, 0, 8, stream_));
+    enqueue_step(false, nullptr, true);
+    FLK_CUDA(cudaGetLastError());
+    uint32_t err[4];
+    unsigned long long nd = 0;
+    FLK_CUDA(cudaMemcpyAsync(err, err64_, 16, cudaMemcpyDeviceToHost, stream_));
+    FLK_CUDA(cudaMemcpyAsync(&nd, ndue64_, 8, cudaMemcpyDeviceToHost, stream_));
+    std::vector<double> o64((size_t)V_ * 15);
+    FLK_CUDA(cudaMemcpyAsync(o64.data(), out64_, o64.size() * 8, cudaMemcpyDeviceToHost, stream_));
+    std::vector<uint32_t> ids[2];
+    for (int k = 0; k < 2; ++k) {
+        ids[k].resize(used_);
+        if (used_)
+            FLK_CUDA(cudaMemcpyAsync(ids[k].data(), ar_.id + (size_t)k * cap_, (size_t)used_ * 4,
+                                     cudaMemcpyDeviceToHost, stream_));
+    }
+    FLK_CUDA(cudaStreamSynchronize(stream_));
+    float ep, ev;
+    std::memcpy(&ep, &err[0], 4);
+    std::memcpy(&ev, &err[1], 4);
+    report[0] = ep;
+    report[1] = ev;
+    report[2] = err[2];
+    report[3] = (double)nd;
+    for (const FlockDesc& d : before) {
+        std::vector<double> w;
+        if (d.remaining) {
+            // view index vbase + i sits in slot sbase + i of the copy the step wrote
+            const std::vector<uint32_t>& nid = ids[(d.parity & 1u) ^ 1u];
+            w.resize((size_t)d.n * 15);
+            for (uint32_t i = 0; i < d.n; ++i) {
+                const uint32_t bird = nid[d.sbase + i];
+                if (bird >= d.n) throw Error{-6, "bird index out of range in step_f64"};
+                std::memcpy(&w[(size_t)bird * 15], &o64[(size_t)(d.vbase + i) * 15], 15 * 8);
+            }
+        }
+        out->push_back(std::move(w));
+    }
 }
 
 void Engine::sync() {

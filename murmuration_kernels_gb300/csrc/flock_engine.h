@@ -137,6 +137,12 @@ public:
     void run_timed(uint32_t steps, uint32_t warmup, PassTimes* out);
     // One eager step that also returns every flock's grid and set summaries.
     void step_debug(std::vector<GridDebug>* out);
+    // One production step of every active flock that also evaluates the same
+    // step in FP64 from the same input state. out[k] (per table flock, bird
+    // order, n*15) receives the FP64 post-step state; report = {max relative
+    // position error, max relative velocity error, neighbour-count
+    // mismatches, deciding birds} of the f32 step against it.
+    void step_f64(std::vector<std::vector<double>>* out, double report[4]);
     void sync();
     uint32_t check_device_error();  // returns and clears the device error word
 
@@ -164,7 +170,7 @@ private:
     void rebuild_table(bool grid_output);
     void prepare(bool grid_output);  // rebuild the table if stale or built for the other mode
     void ensure_scratch();
-    void enqueue_step(bool sets, cudaEvent_t* ev = nullptr);
+    void enqueue_step(bool sets, cudaEvent_t* ev = nullptr, bool f64 = false);
     void free_graphs();
     void ensure_graph();
     void sync_times();
@@ -204,6 +210,14 @@ private:
     float* radius_table_ = nullptr;
     float* staging_ = nullptr;
     size_t staging_cap_ = 0;
+    // FP64 evaluation (allocated on first use): decisions, post-step state,
+    // per-flock active flags, error words
+    double *dec64_ = nullptr, *out64_ = nullptr;
+    uint32_t f64_V_ = 0;
+    uint8_t* active_ = nullptr;
+    uint32_t active_cap_ = 0;
+    uint32_t* err64_ = nullptr;
+    unsigned long long* ndue64_ = nullptr;
 
     cudaGraphExec_t graph_ = nullptr;
     uint32_t graph_steps_ = 0;

@@ -543,3 +543,38 @@ def test_pool_snapshot_and_restore_continue_exactly(native, tmp_path):
         t_end, w_end, _ = pool.wait(t_run)
         assert kf == 2000 and tf == t_end and wf.tobytes() == w_end.tobytes()
         pool.wait(t_wait)
+
+
+@pytest.mark.parametrize("n,seed,settle", [(2000, 1, 0), (30_000, 5, 40), (100_000, 1, 0)])
+def test_fp64_step_matches_the_oracle_fp64_twin(native, oracle, n, seed, settle):
+    """flk_step_f64: the FP64 evaluation equals the oracle's FP64 twin from the
+    same input (same sets, so exact counts, next decisions, and values to
+    double rounding), the flock advances exactly as step(1), and the report
+    is the f32 step's error against FP64."""
+    w = oracle.scatter(n, seed)
+    t0 = 0.0
+    if settle:
+        t0, w = oracle.steps(w, 0.0, settle)
+    f = native.Flock(w, t0)
+    out, rep = f.step_f64()
+    tf, g = f.read()
+    f.close()
+    p = native.Flock(w, t0)
+    p.step(1)
+    tp, gp = p.read()
+    p.close()
+    assert tf == tp and g.tobytes() == gp.tobytes()
+    d = oracle.step_f64(w, t0)
+    assert np.array_equal(out[:, 13], d[:, 13]), "FP64 neighbour counts"
+    assert np.array_equal(out[:, 12], d[:, 12]), "FP64 next decisions"
+    rel = lambda a, b: np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-6)
+    assert rel(out[:, 0:3], d[:, 0:3]).max() <= 1e-12
+    assert rel(out[:, 3:6], d[:, 3:6]).max() <= 1e-12
+    assert np.abs(out[:, 9:12] - d[:, 9:12]).max() <= 1e-9
+    assert np.abs(out[:, 8] - d[:, 8]).max() <= 1e-12
+    # the report: the f32 step against the FP64 one, the bar of the parity tests
+    e_pos = rel(g[:, 0:3].astype(np.float64), d[:, 0:3]).max()
+    assert rep["max_rel_pos"] == pytest.approx(e_pos, rel=1e-3, abs=1e-12)
+    assert 0 < rep["max_rel_pos"] <= REL_TOL and rep["max_rel_vel"] <= REL_TOL
+    assert rep["deciding"] == int((np.float32(np.float32(t0) + np.float32(0.005)) >= w[:, 12]).sum())
+    assert rep["neighbour_mismatches"] == int((g[:, 13].view(np.uint32) != d[:, 13]).sum())
