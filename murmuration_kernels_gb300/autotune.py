@@ -23,11 +23,11 @@ from typing import Optional
 
 SPACE = {
     "stream_bps": [4, 8, 16],
-    "decide_bps": [4, 8, 16],
-    "decide_threads": [128, 256],
+    "decide_bps": [1, 2, 4, 8],
+    "decide_threads": [256, 512, 1024],
     "graph_chunk": [5, 10, 20],
 }
-DEFAULT = {"stream_bps": 8, "decide_bps": 8, "decide_threads": 256, "graph_chunk": 10}
+DEFAULT = {"stream_bps": 8, "decide_bps": 1, "decide_threads": 1024, "graph_chunk": 10}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 

@@ -55,7 +55,7 @@ def commands(verbose_ptxas: bool = False) -> tuple[list[list[str]], list[list[st
           "-c", os.path.join(CSRC, "flock_engine.cu"), "-o", eng_o]
     if verbose_ptxas:
         cu.insert(1, "-Xptxas=-v")
-    # extra nvcc flags for launch-shape experiments, e.g. FLK_NVCC_FLAGS=-DFLK_DECIDE_MIN_BLOCKS=3
+    # extra nvcc flags, e.g. FLK_NVCC_FLAGS=-Xptxas=-v for register and spill reports
     extra = os.environ.get("FLK_NVCC_FLAGS", "").split()
     cu[1:1] = extra
     cu_na = cu[:cu.index("-c")] + ["-c", os.path.join(CSRC, "flock_noalloc.cu"), "-o", noalloc_o]

@@ -85,8 +85,8 @@ struct PassTimes {
 // Sizes of the engine's launch shapes; chosen by the autotuner or defaults.
 struct LaunchShape {
     int stream_blocks_per_sm = 8;   // bird-parallel passes: 256-thread CTAs per SM
-    int decide_threads = 256;       // threads per decide CTA
-    int decide_blocks_per_sm = 8;   // decide CTAs per SM
+    int decide_threads = 1024;      // threads per decide CTA
+    int decide_blocks_per_sm = 1;   // decide CTAs per SM
     int segsort_blocks_per_sm = 8;  // segment-sort CTAs per SM (256 threads)
     int graph_chunk = 10;           // steps per captured CUDA graph
 };

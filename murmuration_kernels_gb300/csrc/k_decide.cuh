@@ -304,10 +304,6 @@ __device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot,
     }
 }
 
-// CTAs of 256 threads the register budget is sized for (4 -> 64 registers).
-#ifndef FLK_DECIDE_MIN_BLOCKS
-#define FLK_DECIDE_MIN_BLOCKS 4
-#endif
 
 // Bucket of cell (cx, cy, cz): SETS steps report their grid and use the
 // reference hash; production steps use the lattice index.
@@ -316,9 +312,13 @@ __device__ __forceinline__ uint32_t bucket_of(int cx, int cy, int cz, uint32_t b
     return SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u)) : lattice_bucket(cx, cy, cz, buckets);
 }
 
-// Dynamic shared memory: one WarpSmem<SETS> per warp.
+// Dynamic shared memory: one WarpSmem<SETS> per warp. 64 registers per
+// thread, so one 1024-thread CTA fills an SM; with that shape all 32 warps of
+// an SM take consecutive due records, i.e. neighbouring birds, and share their
+// candidates in L1 (0.221 -> 0.203 ms at 1M birds against four 256-thread
+// CTAs per SM, which take records from four distant places).
 template <bool SETS>
-__global__ void __launch_bounds__(256, FLK_DECIDE_MIN_BLOCKS) k_decide(const FlockDesc* __restrict__ fl, int nfl,
+__global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict__ fl, int nfl,
                                                                       uint32_t V, StepCtl* __restrict__ ctl,
                                                                       const DueRec* __restrict__ due,
                                                                       const uint32_t* __restrict__ offsets,
