@@ -205,6 +205,53 @@ __device__ __forceinline__ void sweep_ranges(Sweep& w, uint32_t km, uint32_t s, 
     }
 }
 
+// Cheap phase over the fast path's bucket ranges, packed: the ranges (one
+// per lane, in lane order) are concatenated and swept 32 candidates at a time
+// across range boundaries, two chunks per iteration. The candidates come in
+// exactly the order of a range-by-range sweep, so the hit queue, and every
+// sum, is unchanged; short ranges just stop wasting lanes. A lane finds the
+// range of its candidate i from the bitmask of ranges starting in its chunk.
+template <bool SETS>
+__device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, uint32_t lane) {
+    const uint32_t nz = __ballot_sync(FULL, e > s);
+    const uint32_t R = __popc(nz);
+    if (!R) return;
+    // lane q takes the q-th non-empty range
+    const int src = lane < R ? (int)__fns(nz, 0, (int)lane + 1) : 0;
+    const uint32_t rs = __shfl_sync(FULL, s, src);
+    uint32_t rl = __shfl_sync(FULL, e - s, src);
+    if (lane >= R) rl = 0;
+    uint32_t inc = rl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, inc, o);
+        if ((int)lane >= o) inc += y;
+    }
+    const uint32_t T = __shfl_sync(FULL, inc, 31);  // candidates in all
+    const uint32_t P = inc - rl;                     // where this lane's range starts in the concatenation
+    const uint32_t D = rs - P;                       // candidate i of this range is view index i + D
+    uint32_t lemask;
+    asm("mov.u32 %0, %%lanemask_le;" : "=r"(lemask));
+    uint32_t r0 = 0;  // ranges started before the current chunk
+    for (uint32_t c0 = 0; c0 < T; c0 += 64) {
+        const uint32_t bA = __reduce_or_sync(FULL, lane < R && P - c0 < 32u ? 1u << (P - c0) : 0u);
+        const uint32_t bB = __reduce_or_sync(FULL, lane < R && P - (c0 + 32) < 32u ? 1u << (P - c0 - 32) : 0u);
+        const uint32_t iA = c0 + lane, iB = iA + 32;
+        const uint32_t rA = r0 + __popc(bA & lemask) - 1;
+        const uint32_t rB = r0 + __popc(bA) + __popc(bB & lemask) - 1;
+        const uint32_t tA = iA + __shfl_sync(FULL, D, rA & 31), tB = iB + __shfl_sync(FULL, D, rB & 31);
+        r0 += __popc(bA) + __popc(bB);
+        const bool vA = iA < T && tA != w.self, vB = iB < T && tB != w.self;
+        float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
+        if (vA) qA = __ldg(&w.pos[tA + w.shift]);
+        if (vB) qB = __ldg(&w.pos[tB + w.shift]);
+        const bool hA = vA && near<false>(w, qA, 0, 0, 0);
+        const bool hB = vB && near<false>(w, qB, 0, 0, 0);
+        enqueue<SETS>(w, hA, tA, lane);
+        enqueue<SETS>(w, hB, tB, lane);
+    }
+}
+
 template <bool SETS>
 __device__ __forceinline__ void drain(Sweep& w, uint32_t lane) {
     if (w.qn) {
@@ -396,7 +443,7 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             uint32_t s = 0, en = 0;
             if (keep) bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
             cand += en - s;
-            sweep_ranges<SETS>(w, __ballot_sync(FULL, en > s), s, en, lane);
+            sweep_packed<SETS>(w, s, en, lane);
         } else {
             // the flock's own view region [vbase, vbase + n)
             const FlockDesc* fd = &fl[find_flock_v(fl, nfl, k)];
