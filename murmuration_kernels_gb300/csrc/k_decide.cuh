@@ -146,6 +146,18 @@ __device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int
     return hit;
 }
 
+// near<false> for two candidates at once with paired f32 arithmetic (each
+// element rounded to nearest, so bit-identical to two scalar tests).
+__device__ __forceinline__ void near2(const Sweep& w, const float4 qa, const float4 qb, bool& ha, bool& hb) {
+    const float2 np = make_float2(-w.p.x, -w.p.x), nq = make_float2(-w.p.y, -w.p.y), nr = make_float2(-w.p.z, -w.p.z);
+    const float2 dx = __fadd2_rn(make_float2(qa.x, qb.x), np);
+    const float2 dy = __fadd2_rn(make_float2(qa.y, qb.y), nq);
+    const float2 dz = __fadd2_rn(make_float2(qa.z, qb.z), nr);
+    const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+    ha = d2.x <= w.c2;
+    hb = d2.y <= w.c2;
+}
+
 // Cheap phase over one contiguous candidate range [sc, ec) (wide paths).
 template <bool SETS, bool CHECK_CELL>
 __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32_t lane, int cx = 0, int cy = 0,
@@ -245,8 +257,10 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
         float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
         if (vA) qA = __ldg(&w.pos[tA + w.shift]);
         if (vB) qB = __ldg(&w.pos[tB + w.shift]);
-        const bool hA = vA && near<false>(w, qA, 0, 0, 0);
-        const bool hB = vB && near<false>(w, qB, 0, 0, 0);
+        bool hA, hB;
+        near2(w, qA, qB, hA, hB);
+        hA = hA && vA;
+        hB = hB && vB;
         enqueue<SETS>(w, hA, tA, lane);
         enqueue<SETS>(w, hB, tB, lane);
     }
