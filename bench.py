@@ -267,6 +267,30 @@ def bench_plain(m, args, dist, local):
                 pairs_per_due=(pairs1 - pairs0) / max(1, due1 - due0), due_total=due0)
 
 
+def decide_rates(r, n):
+    """decide's work rates over the eager passes' decide time: candidate tests/s
+    and true pairs (within 2R) per second, with the per-bird figures."""
+    due_per_step = r["due_frac"] * n
+    dec_s = r["passes"]["decide_ms"] / 1e3
+    return {"candidates_per_deciding_bird": r["cand_per_due"], "pairs_in_2R_per_deciding_bird": r["pairs_per_due"],
+            "deciding_per_step": due_per_step,
+            "candidate_tests_per_s": r["cand_per_due"] * due_per_step / dec_s if dec_s > 0 else None,
+            "pairs_per_s": r["pairs_per_due"] * due_per_step / dec_s if dec_s > 0 else None}
+
+
+def pass_bandwidths(r, n):
+    """Algorithmic bytes of each streaming pass / its eager time (GB/s): hash reads
+    a position and writes key + rank (24 B/bird); scatter + sort read key, rank,
+    bird index, sort key and the state and write the state, heading and the
+    deciding birds' records (8+4+4+8+68 + 8+68+16 + 48 f B/bird); integrate
+    reads position, velocity, steering and writes position, velocity (80 B/bird)."""
+    p, f = r["passes"], r["due_frac"]
+    def gbs(bytes_per_bird, ms):
+        return round(bytes_per_bird * n / (ms / 1e3) / 1e9, 1) if ms > 0 else None
+    return {"hash": gbs(24, p["hash_ms"]), "scatter_sort": gbs(184 + 48 * f, p["sort_ms"]),
+            "integrate": gbs(80, p["integrate_ms"])}
+
+
 def bench_e2e(m, args, local):
     """Through the C ABI with host buffers: upload, K steps, download."""
     n, K = args.birds, args.steps
@@ -426,8 +450,8 @@ def main():
                      "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,
                      "traffic": traffic},
         "passes_ms": {k: round(v, 5) for k, v in r["passes"].items() if k.endswith("_ms")},
-        "decide": {"candidates_per_deciding_bird": r["cand_per_due"], "pairs_in_2R_per_deciding_bird":
-                   r["pairs_per_due"]},
+        "decide": decide_rates(r, n),
+        "passes_gbs": pass_bandwidths(r, n),
         "gpu_launches": m.kernels_per_step() * K,
         "clocks": r["clocks"],
         "step_ms_p50": float(np.median(r["ms"])), "step_ms_min": float(r["ms"].min()),
