@@ -346,14 +346,38 @@ __device__ __forceinline__ void bitonic_lanes(T (&x)[R], uint32_t lane) {
     }
 }
 
+// A warp's deciding-bird records wait in shared memory and reach the global
+// list in batches, one atomic on the list's counter per batch instead of one
+// per bucket (that single counter was hit ~30,000 times per step at 1M birds).
+constexpr uint32_t DUE_STAGE = 64;  // records per warp; flushed once more than 32 wait
+
+struct DueStage {
+    DueRec* rec;   // this warp's DUE_STAGE records in shared memory
+    uint32_t n;    // records waiting (warp-uniform)
+};
+
+__device__ __forceinline__ void flush_due(DueStage& sg, uint32_t lane, DueRec* __restrict__ due,
+                                          StepCtl* __restrict__ ctl) {
+    if (!sg.n) return;
+    __syncwarp();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->due_count, sg.n);
+    base = __shfl_sync(FULL, base, 0);
+    const uint4* src = reinterpret_cast<const uint4*>(sg.rec);
+    uint4* dst = reinterpret_cast<uint4*>(due + base);
+    for (uint32_t i = lane; i < sg.n * 3; i += 32) dst[i] = src[i];
+    __syncwarp();
+    sg.n = 0;
+}
+
 // Moves one bird (sort key x = bird << 32 | old view index) to view index
 // `pos` of the reordered buffer, writes its unit heading to the forward view
-// and, when it decides this step, its self-contained decide record. Called by
-// all 32 lanes.
+// and, when it decides this step, stages its self-contained decide record.
+// Called by all 32 lanes.
 __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned long long x, const FlockDesc& d,
                                             float t_now, uint32_t lane, const Arena& ar, uint32_t oshift,
-                                            uint32_t nshift, float4* __restrict__ sfwd, DueRec* __restrict__ due,
-                                            StepCtl* __restrict__ ctl) {
+                                            uint32_t nshift, float4* __restrict__ sfwd, DueStage& sg,
+                                            DueRec* __restrict__ due, StepCtl* __restrict__ ctl) {
     bool is_due = false;
     uint32_t nst = 0;
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), c = a;
@@ -377,16 +401,15 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned lon
     }
     const uint32_t dm = __ballot_sync(FULL, is_due);
     if (dm) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&ctl->due_count, (uint32_t)__popc(dm));
-        base = __shfl_sync(FULL, base, 0);
         if (is_due) {
             DueRec r;
             r.pr = make_float4(a.x, a.y, a.z, c.w);
             r.fk = make_float4(fw.x, fw.y, fw.z, __uint_as_float(pos));
             r.fl = make_uint4(nst, d.bbase, d.buckets, nshift);
-            due[base + __popc(dm & lanemask_lt())] = r;
+            sg.rec[sg.n + __popc(dm & lanemask_lt())] = r;
         }
+        sg.n += __popc(dm);
+        if (sg.n > DUE_STAGE - 32) flush_due(sg, lane, due, ctl);
     }
 }
 
@@ -397,11 +420,17 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
                                                  const unsigned long long* __restrict__ tmp, Arena ar,
                                                  float4* __restrict__ sfwd, DueRec* __restrict__ due) {
     constexpr unsigned long long PAD = ~0ull;
+    __shared__ DueRec s_due[8][DUE_STAGE];  // 256-thread CTAs: 8 warps
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
-    for (uint32_t w = gw; w < nocc; w += nw) {
+    DueStage sg{s_due[(threadIdx.x >> 5) & 7], 0u};
+    // each warp takes a contiguous range of occupied buckets (neighbouring
+    // cells), so a batch of staged records stays spatially close for decide
+    const uint32_t per = (nocc + nw - 1) / nw;
+    const uint32_t w_end = min(nocc, gw * per + per);
+    for (uint32_t w = gw * per; w < w_end; ++w) {
         const uint32_t b = occ[w];
         const int f = find_flock_b(fl, nfl, b);
         const FlockDesc d = fl[f];
@@ -417,7 +446,7 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
         if (L <= 32) {
             unsigned long long x = lane < L ? tmp[s0 + lane] : PAD;
             x = bitonic32(x, lane);
-            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, due, ctl);
+            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
         } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
             unsigned long long x[2];
 #pragma unroll
@@ -425,8 +454,8 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             bitonic_lanes<2>(x, lane);
 #pragma unroll
             for (int k = 0; k < 2; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, due,
-                            ctl);
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
+                            due, ctl);
         } else if (L <= 128) {
             unsigned long long x[4];
 #pragma unroll
@@ -434,8 +463,8 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             bitonic_lanes<4>(x, lane);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, due,
-                            ctl);
+                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
+                            due, ctl);
         } else {
             // long range (dense cell or hash collision): rank by counting; bird
             // indices are distinct within a flock, so ranks are distinct
@@ -449,10 +478,11 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
 #pragma unroll 8
                     for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < xb;
                 }
-                emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, due, ctl);
+                emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
             }
         }
     }
+    flush_due(sg, lane, due, ctl);
 }
 
 }  // namespace flk
