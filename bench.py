@@ -320,13 +320,21 @@ def bench_batched(m, args, local):
     K = args.batched_steps
     flocks = [m.generate(int(nf), 3 + k) for k, nf in enumerate(sizes)]
     total = int(sizes.sum())
+    from murmuration_kernels_gb300 import autotune
+
+    # launch shapes for this mix, tuned on a copy: the tuner's trials advance
+    # the flocks, and the timed batch must start from the same states as the
+    # one-at-a-time runs below
+    t = m.Batch(device=local)
+    for w in flocks:
+        t.add(w)
+    tuned = autotune.tune(t, steps=10, use_cache=False)
+    t.close()
     b = m.Batch(device=local)
     for w in flocks:
         b.add(w)
-    from murmuration_kernels_gb300 import autotune
-
-    tuned = autotune.tune(b, steps=10, use_cache=False)  # launch shapes for this mix
-    b.step(10)  # warm-up (graph capture)
+    b.tune(**{k: v for k, v in tuned["shape"].items()})
+    b.step(10)  # warm-up (graph capture), as the one-at-a-time runs
     ms_batched = b.time_steps(K)
     passes = b.step_timed(5, 0)
     b.close()
