@@ -7,19 +7,26 @@
 //
 //   k_hash_count  cell key per bird + bucket histogram with warp-aggregated
 //                 atomics (__match_any_sync); records each bird's arrival rank
-//                 and appends first-seen buckets to an occupied-bucket list.
-//   k_scan        single-pass decoupled look-back exclusive scan of the
-//                 histogram into bucket offsets (buckets+1 entries); it also
-//                 zeroes the histogram for the next step. Bounded waits.
-//   k_scatter     bird -> slot in its bucket's range (arrival order).
-//   k_segsort     one warp per occupied bucket sorts its range by bird index
-//                 (the canonical stable order) and moves those birds' state
-//                 into the other of the flock's two state buffers in that
-//                 order; it also writes each bird's unit heading and the
-//                 deciding-bird list.
-//   k_decide      one warp per deciding bird: the 2R neighbourhood's buckets
-//                 are deduplicated with __match_any_sync, lanes sweep each
-//                 bucket's contiguous float4 range, and warp shuffles reduce.
+//                 and appends first-seen buckets to an occupied-bucket list
+//                 (one atomic per CTA iteration). Production steps bucket
+//                 cells by a lattice index, grid-reporting steps by the
+//                 reference's hash.
+//   k_alloc       production steps: each occupied bucket's run start from a
+//                 per-flock cursor (one atomic per warp).
+//   k_scan        grid-reporting steps: single-pass decoupled look-back
+//                 exclusive scan of the histogram into the canonical dense
+//                 offsets (buckets+1 entries). Bounded waits.
+//   k_scatter     bird -> slot in its bucket's run (arrival order).
+//   k_segsort     one warp per occupied bucket (contiguous ranges of them per
+//                 warp) sorts its run by bird index (the canonical stable
+//                 order) and moves those birds' state into the other of the
+//                 flock's two state buffers in that order; it also writes each
+//                 bird's unit heading and stages the deciding-bird records.
+//   k_decide      one warp per deciding bird, one 1024-thread CTA per SM: the
+//                 2R neighbourhood's buckets (deduplicated with
+//                 __match_any_sync) are swept as one packed sequence of
+//                 candidates, hits are queued and processed on full warps,
+//                 and a reduce-scatter of shuffles sums them.
 //   k_integrate   banked flight, streaming float4 over the reordered buffer;
 //                 its last block advances the flock clocks, makes the
 //                 reordered buffer current and resets the step counters.

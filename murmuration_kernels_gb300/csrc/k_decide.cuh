@@ -11,16 +11,16 @@
 //
 // Each bucket's birds are contiguous in the flock's state, which the sort
 // pass has just written in cell order (view index t lives in slot t + shift of
-// the reordered buffer), so the lanes of a warp read one coalesced 512 B run
-// of positions per cell. The sweep is split in
-// two: the cheap phase computes d2 for every candidate and appends the indices
-// of those within 2R to a per-warp queue in shared memory (ballot + popc);
-// whenever 32 hits are queued, the whole warp processes them together in the
-// expensive phase (sqrt, three IEEE divisions, the separation Gaussian,
-// blind-angle test). Only ~11 % of candidates are hits, so this keeps the
-// expensive code on full warps instead of running it for one or two lanes.
-// The cheap phase walks the neighbourhood two 32-candidate chunks at a time so
-// each lane has two loads in flight.
+// the reordered buffer), so the lanes of a warp read coalesced runs of
+// positions. The sweep is split in two: the cheap phase computes d2 for every
+// candidate and appends the indices of those within 2R to a per-warp queue in
+// shared memory (ballot + popc); whenever 32 hits are queued, the whole warp
+// processes them together in the expensive phase (sqrt, three IEEE divisions,
+// the separation Gaussian, blind-angle test). Only ~14 % of candidates are
+// hits, so this keeps the expensive code on full warps instead of running it
+// for one or two lanes. The cheap phase sweeps the bucket ranges as one packed
+// sequence, two 32-candidate chunks per iteration (two loads in flight per
+// lane, tested together with paired f32x2 arithmetic).
 //
 // Per-lane partial sums are reduced with a transposed (reduce-scatter)
 // shuffle pattern straight into shared memory; once 32 birds are reduced, all
