@@ -277,17 +277,27 @@ __device__ __forceinline__ void drain(Sweep& w, uint32_t lane) {
 }
 
 // Reduce-scatter of K = 2^m values across the warp: afterwards lane l holds the
-// warp total of value index (l >> (5 - m)) & (K - 1) (fixed association).
+// warp total of value index (l >> (5 - m)) & (K - 1) (fixed association). The
+// float version adds value pairs with f32x2 (each element rounded to nearest).
 template <int K>
 __device__ __forceinline__ float rs_float(float (&v)[K], uint32_t lane) {
 #pragma unroll
     for (int half = K / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
         const bool upper = (lane & o) != 0;
+        if (half >= 2) {
 #pragma unroll
-        for (int i = 0; i < half; ++i) {
-            const float send = upper ? v[i] : v[i + half];
-            const float keep = upper ? v[i + half] : v[i];
-            v[i] = __fadd_rn(keep, __shfl_xor_sync(FULL, send, o));
+            for (int i = 0; i < half; i += 2) {
+                const float s0 = upper ? v[i] : v[i + half], s1 = upper ? v[i + 1] : v[i + 1 + half];
+                const float k0 = upper ? v[i + half] : v[i], k1 = upper ? v[i + 1 + half] : v[i + 1];
+                const float2 r = __fadd2_rn(make_float2(k0, k1),
+                                            make_float2(__shfl_xor_sync(FULL, s0, o), __shfl_xor_sync(FULL, s1, o)));
+                v[i] = r.x;
+                v[i + 1] = r.y;
+            }
+        } else {
+            const float send = upper ? v[0] : v[1];
+            const float keep = upper ? v[1] : v[0];
+            v[0] = __fadd_rn(keep, __shfl_xor_sync(FULL, send, o));
         }
     }
 #pragma unroll
@@ -438,9 +448,18 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             bool valid = false;
             uint32_t b = 0;
             if ((long long)lane < ncell) {
-                const int cx = lx + (int)lane % nx;
-                const int t = (int)lane / nx;
-                const int cy = ly + t % ny, cz = lz + t / ny;
+                // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift:
+                // floor(x / d) = (x * m) >> 16 with m = floor(65536 / d) + 1 holds for
+                // x < 32 and d <= 32 (m exceeds 65536 / d by at most 1, so the error
+                // x / 65536 < 1 / d never reaches the next integer); floor(65536 / d)
+                // from an approximate f32 quotient is exact here, since 65536 / d is
+                // a power of two or at least 1/32 away from an integer.
+                const uint32_t mx = __float2uint_rz(__fdividef(65536.0f, (float)nx)) + 1u;
+                const uint32_t my = __float2uint_rz(__fdividef(65536.0f, (float)ny)) + 1u;
+                const uint32_t t = (lane * mx) >> 16;
+                const uint32_t iz = (t * my) >> 16;
+                const int cx = lx + (int)(lane - t * (uint32_t)nx);
+                const int cy = ly + (int)(t - iz * (uint32_t)ny), cz = lz + (int)iz;
                 const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
                 const float dx = fminf(fmaxf(p.x, ox), ox + GRID_CELL) - p.x;
                 const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
