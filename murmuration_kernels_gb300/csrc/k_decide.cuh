@@ -245,18 +245,20 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
     uint32_t lemask;
     asm("mov.u32 %0, %%lanemask_le;" : "=r"(lemask));
     uint32_t r0 = 0;  // ranges started before the current chunk
-    for (uint32_t c0 = 0; c0 < T; c0 += 64) {
-        const uint32_t bA = __reduce_or_sync(FULL, lane < R && P - c0 < 32u ? 1u << (P - c0) : 0u);
-        const uint32_t bB = __reduce_or_sync(FULL, lane < R && P - (c0 + 32) < 32u ? 1u << (P - c0 - 32) : 0u);
+    // the chunk this lane's range starts in, and its bit there (lanes >= R: none)
+    const uint32_t pch = lane < R ? P >> 5 : 0xFFFFFFFFu, pbit = 1u << (P & 31u);
+    for (uint32_t c0 = 0, ch = 0; c0 < T; c0 += 64, ch += 2) {
+        const uint32_t bA = __reduce_or_sync(FULL, pch == ch ? pbit : 0u);
+        const uint32_t bB = __reduce_or_sync(FULL, pch == ch + 1 ? pbit : 0u);
         const uint32_t iA = c0 + lane, iB = iA + 32;
         const uint32_t rA = r0 + __popc(bA & lemask) - 1;
         const uint32_t rB = r0 + __popc(bA) + __popc(bB & lemask) - 1;
         const uint32_t tA = iA + __shfl_sync(FULL, D, rA & 31), tB = iB + __shfl_sync(FULL, D, rB & 31);
         r0 += __popc(bA) + __popc(bB);
         const bool vA = iA < T && tA != w.self, vB = iB < T && tB != w.self;
-        float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
-        if (vA) qA = __ldg(&w.pos[tA + w.shift]);
-        if (vB) qB = __ldg(&w.pos[tB + w.shift]);
+        // invalid lanes read the bird's own slot (always in range) and discard it
+        const float4 qA = __ldg(&w.pos[(vA ? tA : w.self) + w.shift]);
+        const float4 qB = __ldg(&w.pos[(vB ? tB : w.self) + w.shift]);
         bool hA, hB;
         near2(w, qA, qB, hA, hB);
         hA = hA && vA;
