@@ -78,7 +78,7 @@ struct Sweep {
     const float4* __restrict__ pos;   // state: position, roll (by slot)
     const uint32_t* __restrict__ bid;  // state: bird index (by slot)
     const float4* __restrict__ sfwd;  // unit headings (by view index)
-    uint32_t* q;  // this warp's 64-entry hit queue (shared memory)
+    uint32_t* q;  // this warp's 96-entry hit queue (shared memory)
     uint32_t qn;  // entries queued (warp-uniform)
     Acc a;
 };
@@ -131,6 +131,31 @@ __device__ __forceinline__ void enqueue(Sweep& w, bool hit, uint32_t t, uint32_t
         const uint32_t moved = lane < extra ? w.q[32 + lane] : 0u;
         __syncwarp();
         if (lane < extra) w.q[lane] = moved;
+        __syncwarp();
+        w.qn = extra;
+    }
+}
+
+// Queues two chunks' hits at once (A's, then B's, the order of two single
+// enqueues) and takes full batches of 32. Hit k of the bird still goes to lane
+// k mod 32, so the sums are the same as with one chunk per enqueue.
+template <bool SETS>
+__device__ __forceinline__ void enqueue2(Sweep& w, bool hA, uint32_t tA, bool hB, uint32_t tB, uint32_t lane) {
+    const uint32_t ma = __ballot_sync(FULL, hA), mb = __ballot_sync(FULL, hB);
+    if (!(ma | mb)) return;
+    const uint32_t lt = lanemask_lt(), na = __popc(ma);
+    if (hA) w.q[w.qn + __popc(ma & lt)] = tA;
+    if (hB) w.q[w.qn + na + __popc(mb & lt)] = tB;
+    w.qn += na + __popc(mb);
+    while (w.qn >= 32) {
+        __syncwarp();
+        take<SETS>(w, w.q[lane]);
+        const uint32_t extra = w.qn - 32;
+        const uint32_t m0 = lane < extra ? w.q[32 + lane] : 0u;
+        const uint32_t m1 = lane + 32 < extra ? w.q[64 + lane] : 0u;
+        __syncwarp();
+        if (lane < extra) w.q[lane] = m0;
+        if (lane + 32 < extra) w.q[32 + lane] = m1;
         __syncwarp();
         w.qn = extra;
     }
@@ -263,8 +288,7 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
         near2(w, qA, qB, hA, hB);
         hA = hA && vA;
         hB = hB && vB;
-        enqueue<SETS>(w, hA, tA, lane);
-        enqueue<SETS>(w, hB, tB, lane);
+        enqueue2<SETS>(w, hA, tA, hB, tB, lane);
     }
 }
 
@@ -333,7 +357,7 @@ __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* _
 template <bool SETS>
 struct WarpSmem {
     static constexpr int NI = SETS ? 8 : 4;  // integer sums per bird
-    uint32_t queue[64];
+    uint32_t queue[96];
     float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
     uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
     uint32_t st[32];       // slot of the bird in the reordered buffer
