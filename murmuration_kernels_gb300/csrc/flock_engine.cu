@@ -113,7 +113,7 @@ Engine::~Engine() {
     dfree(ar_.A); dfree(ar_.B); dfree(ar_.C); dfree(ar_.D); dfree(ar_.id);
     dfree(table_d_);
     dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
-    dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_);
+    dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_); dfree(slabs_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
     dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_); dfree(ndue64_);
     if (copy_) cudaStreamDestroy(copy_);
@@ -128,10 +128,10 @@ void Engine::free_graphs() {
 
 size_t Engine::bytes_for(uint32_t n) {
     // state 2 x 68 B (two buffers) + scratch (key, arrival, occ 4 B each; tmp
-    // 8 B; due record 48 B; heading 16 B) + buckets (counts 4 B + offsets 4 B +
-    // status/4096)
+    // 8 B; due record 48 B; heading 16 B) + buckets (counts, offsets, slab
+    // boundaries 4 B each + status/4096)
     const size_t b = production_buckets(n);
-    return (size_t)n * (136 + 84) + b * 8 + (b / SCAN_TILE) * 8 + 256;
+    return (size_t)n * (136 + 84) + b * 12 + (b / SCAN_TILE) * 8 + 256;
 }
 
 void Engine::set_shape(const LaunchShape& s) {
@@ -561,9 +561,10 @@ void Engine::ensure_scratch() {
     }
     if (Btot_ > scratch_B_) {
         const uint32_t nb = Btot_;
-        dev_bytes_ -= (size_t)scratch_B_ * 8 + (scratch_B_ / SCAN_TILE) * 8;
-        dfree(counts_); dfree(offsets_); dfree(status_);
+        dev_bytes_ -= (size_t)scratch_B_ * 12 + (scratch_B_ / SCAN_TILE) * 8;
+        dfree(counts_); dfree(offsets_); dfree(status_); dfree(slabs_);
         counts_ = dalloc<uint32_t>(nb, &dev_bytes_);
+        slabs_ = dalloc<uint32_t>(nb, &dev_bytes_);
         offsets_ = dalloc<uint32_t>((size_t)nb + 1, &dev_bytes_);
         status_ = dalloc<unsigned long long>(nb / SCAN_TILE, &dev_bytes_);
         FLK_CUDA(cudaMemsetAsync(counts_, 0, (size_t)nb * 4, stream_));
@@ -602,7 +603,7 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64) {
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
     k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
-        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, ar_, sfwd_, due_);
+        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, ar_, sfwd_, due_, slabs_);
     if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
         k_decide_f64<<<pgrid(num_sms_, 8, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                       counts_, ar_, dec64_, ndue64_);
@@ -615,10 +616,11 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64) {
                           (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                       counts_, ar_, sfwd_, radius_table_, sets_);
+                                                                       counts_, ar_, sfwd_, radius_table_, sets_, slabs_);
     else
         k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                        counts_, ar_, sfwd_, radius_table_, nullptr);
+                                                                        counts_, ar_, sfwd_, radius_table_, nullptr,
+                                                                        slabs_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
     k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, counts_, occ_, ctl_);
     if (f64) k_compare_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);

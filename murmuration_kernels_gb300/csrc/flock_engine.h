@@ -204,6 +204,7 @@ private:
     DueRec* due_ = nullptr;
     float4* sfwd_ = nullptr;  // unit heading per view index (read by decide)
     uint32_t *counts_ = nullptr, *offsets_ = nullptr;
+    uint32_t* slabs_ = nullptr;  // per bucket: the run's z-slab boundaries (production steps)
     unsigned long long* status_ = nullptr;
     uint32_t* sets_ = nullptr;  // 8 per virtual bird, debug only
     StepCtl* ctl_ = nullptr;

@@ -423,7 +423,8 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                                                                       Arena ar,
                                                                       const float4* __restrict__ sfwd,
                                                                       const float* __restrict__ rtab,
-                                                                      uint32_t* __restrict__ sets) {
+                                                                      uint32_t* __restrict__ sets,
+                                                                      const uint32_t* __restrict__ slabs) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     WarpSmem<SETS>& m = reinterpret_cast<WarpSmem<SETS>*>(s_raw)[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
@@ -473,6 +474,7 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             // fast path: each distinct bucket of the culled box once, no cell check
             bool valid = false;
             uint32_t b = 0;
+            int z0 = 0, z1 = 3;  // production steps: the z-slabs of this lane's cell within reach
             if ((long long)lane < ncell) {
                 // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift:
                 // floor(x / d) = (x * m) >> 16 with m = floor(65536 / d) + 1 holds for
@@ -486,6 +488,10 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                 const uint32_t iz = (t * my) >> 16;
                 const int cx = lx + (int)(lane - t * (uint32_t)nx);
                 const int cy = ly + (int)(t - iz * (uint32_t)ny), cz = lz + (int)iz;
+                if (!SETS) {
+                    z0 = min(3, max(0, (int)floorf(p.z - reach) - 4 * cz));
+                    z1 = min(3, max(0, (int)floorf(p.z + reach) - 4 * cz));
+                }
                 const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
                 const float dx = fminf(fmaxf(p.x, ox), ox + GRID_CELL) - p.x;
                 const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
@@ -500,7 +506,31 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                 keep = (int)lane == __ffs(peers) - 1;
             }
             uint32_t s = 0, en = 0;
-            if (keep) bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
+            if (keep) {
+                // Production runs are ordered by 1 m z-slab within their cell, and
+                // the sort left each run's slab boundaries (birds in slabs < 1, < 2,
+                // < 3; 10 bits each; all ones: untrimmed). A candidate within the
+                // reach has |dz| <= reach and floor is monotonic, so only slabs
+                // z0..z1 of this cell can hold one: the range shrinks to them.
+                // (A bucket shared by two cells of the box would be swept whole, but
+                // production steps never see one: the box spans at most 3 cells per
+                // axis and the lattice index repeats only every 32 or more.)
+                const uint32_t sw = SETS ? 0xFFFFFFFFu : __ldg(&slabs[b]);  // issued with the range's loads
+                bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
+                if (!SETS && en > s && sw != 0xFFFFFFFFu) {
+                    const uint32_t L = en - s;
+                    const uint32_t lo = z0 <= 0 ? 0u : (sw >> (10 * (z0 - 1))) & 1023u;
+                    const uint32_t hi = z1 >= 3 ? L : (sw >> (10 * z1)) & 1023u;
+                    if (hi <= L) {  // else a stale word: keep the run whole
+                        if (lo >= hi) {
+                            en = s;
+                        } else {
+                            en = s + hi;
+                            s += lo;
+                        }
+                    }
+                }
+            }
             cand += en - s;
             sweep_packed<SETS>(w, s, en, lane);
         } else {

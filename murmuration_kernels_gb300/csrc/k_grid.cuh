@@ -53,8 +53,10 @@ __global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t base, Arena s
 // ---------------------------------------------------------------------------
 // pass 1: cell key + histogram (warp-aggregated atomics)
 // ---------------------------------------------------------------------------
-// LATTICE: production bucket function (lattice_bucket); otherwise the
-// reference's cell hash, whose keys a grid-reporting step returns.
+// LATTICE: a production step: lattice_bucket, and the bird's 1 m z-slab in
+// its cell (0..3) rides in the top two bits of its arrival rank, so the sort
+// can order each run by slab. Otherwise the reference's cell hash, whose keys
+// a grid-reporting step returns, and slab 0 for every bird.
 // Each CTA takes 256 consecutive view indices per iteration. Bucket counts
 // use one atomic per distinct bucket of a warp; the occupied-bucket list gets
 // one atomic per CTA iteration (the first-seen buckets of all eight warps are
@@ -72,12 +74,14 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
     for (uint32_t blk = blockIdx.x * blockDim.x; blk < V; blk += stride, it ^= 1u) {
         const uint32_t v = blk + threadIdx.x;
         bool act = false;
-        uint32_t b = 0;
+        uint32_t b = 0, slab = 0;
         if (v < V) {
             const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
             if (__ldg(&d->remaining)) {
                 const float4 p = ar.A[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
                 const int cx = cell1(p.x), cy = cell1(p.y), cz = cell1(p.z);
+                // floor(z) - 4 * floor(z / 4): z * 0.25 is exact, so this agrees with cell1
+                if (LATTICE) slab = (uint32_t)((int)floorf(p.z) - 4 * cz) & 3u;
                 const uint32_t nb = __ldg(&d->buckets);
                 b = __ldg(&d->bbase) + (LATTICE ? lattice_bucket(cx, cy, cz, nb) : (cell_hash(cx, cy, cz) & (nb - 1u)));
                 key[v] = b;
@@ -93,7 +97,8 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
             if ((int)lane == leader) old = atomicAdd(&counts[b], (uint32_t)__popc(peers));
             old = __shfl_sync(m, old, leader);
             const uint32_t rank = old + __popc(peers & lanemask_lt());
-            arrival[v] = rank;
+            if (rank >= (1u << 30)) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);  // 2^30 birds in one cell
+            arrival[v] = (rank & 0x3FFFFFFFu) | (slab << 30);
             first = rank == 0;
         }
         const uint32_t fm = __ballot_sync(FULL, first);
@@ -272,8 +277,10 @@ __global__ void __launch_bounds__(256) k_alloc(FlockDesc* __restrict__ fl, int n
 // ---------------------------------------------------------------------------
 // pass 3: scatter by arrival rank
 // ---------------------------------------------------------------------------
-// Each bird's sort key goes to its slot in its bucket's run: the bird index
-// (the stable order) in the high half, its current view index in the low half.
+// Each bird's sort key goes to its slot in its bucket's run:
+// slab << 62 | bird << 31 | (view index - vbase). Sorting it orders a run by
+// z-slab, then bird index (bird index alone in grid-reporting steps, whose
+// slabs are all 0). Bird and local view index are below 2^31.
 __global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
                                                  const uint32_t* __restrict__ key, const uint32_t* __restrict__ arrival,
                                                  const uint32_t* __restrict__ offsets,
@@ -282,8 +289,11 @@ __global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ f
         const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
         if (!__ldg(&d->remaining)) continue;
         const uint32_t bird = ar.id[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
-        const uint32_t pos = __ldg(&offsets[key[v]]) + arrival[v];
-        if (pos < V) tmp[pos] = ((unsigned long long)bird << 32) | v;
+        const uint32_t arr = arrival[v];
+        const uint32_t pos = __ldg(&offsets[key[v]]) + (arr & 0x3FFFFFFFu);
+        if (pos < V)
+            tmp[pos] = ((unsigned long long)(arr >> 30) << 62) | ((unsigned long long)bird << 31) |
+                       (unsigned long long)(v - __ldg(&d->vbase));
         else atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
     }
 }
@@ -356,6 +366,15 @@ struct DueStage {
     uint32_t n;    // records waiting (warp-uniform)
 };
 
+// Adds the lanes' birds in slabs 0, 0-1 and 0-2 to c1, c2, c3 (warp-uniform).
+__device__ __forceinline__ void slab_counts(bool has, unsigned long long x, uint32_t& c1, uint32_t& c2,
+                                            uint32_t& c3) {
+    const uint32_t sl = (uint32_t)(x >> 62);
+    c1 += __popc(__ballot_sync(FULL, has && sl < 1u));
+    c2 += __popc(__ballot_sync(FULL, has && sl < 2u));
+    c3 += __popc(__ballot_sync(FULL, has && sl < 3u));
+}
+
 __device__ __forceinline__ void flush_due(DueStage& sg, uint32_t lane, DueRec* __restrict__ due,
                                           StepCtl* __restrict__ ctl) {
     if (!sg.n) return;
@@ -370,7 +389,7 @@ __device__ __forceinline__ void flush_due(DueStage& sg, uint32_t lane, DueRec* _
     sg.n = 0;
 }
 
-// Moves one bird (sort key x = bird << 32 | old view index) to view index
+// Moves one bird (sort key x = slab << 62 | bird << 31 | old local view index) to view index
 // `pos` of the reordered buffer, writes its unit heading to the forward view
 // and, when it decides this step, stages its self-contained decide record.
 // Called by all 32 lanes.
@@ -383,8 +402,8 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned lon
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), c = a;
     f3 fw = mk(0.f, 0.f, 0.f);
     if (has) {
-        const uint32_t bird = (uint32_t)(x >> 32);
-        const uint32_t ost = (uint32_t)x + oshift;
+        const uint32_t bird = (uint32_t)(x >> 31) & 0x7FFFFFFFu;
+        const uint32_t ost = d.vbase + ((uint32_t)x & 0x7FFFFFFFu) + oshift;
         nst = pos + nshift;
         a = ar.A[ost];
         const float4 b = ar.B[ost];
@@ -418,7 +437,8 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
                                                  const uint32_t* __restrict__ counts,
                                                  const unsigned long long* __restrict__ tmp, Arena ar,
-                                                 float4* __restrict__ sfwd, DueRec* __restrict__ due) {
+                                                 float4* __restrict__ sfwd, DueRec* __restrict__ due,
+                                                 uint32_t* __restrict__ slabs) {
     constexpr unsigned long long PAD = ~0ull;
     __shared__ DueRec s_due[8][DUE_STAGE];  // 256-thread CTAs: 8 warps
     const uint32_t lane = threadIdx.x & 31;
@@ -443,15 +463,20 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
             continue;
         }
+        uint32_t c1 = 0, c2 = 0, c3 = 0;
         if (L <= 32) {
             unsigned long long x = lane < L ? tmp[s0 + lane] : PAD;
             x = bitonic32(x, lane);
+            slab_counts(lane < L, x, c1, c2, c3);
             emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
         } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
             unsigned long long x[2];
 #pragma unroll
             for (int k = 0; k < 2; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
             bitonic_lanes<2>(x, lane);
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
 #pragma unroll
             for (int k = 0; k < 2; ++k)
                 emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
@@ -463,6 +488,9 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             bitonic_lanes<4>(x, lane);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
+                slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
                 emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
                             due, ctl);
         } else {
@@ -471,16 +499,18 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
             for (uint32_t c0 = 0; c0 < L; c0 += 32) {
                 const bool has = c0 + lane < L;
                 const unsigned long long x = has ? tmp[s0 + c0 + lane] : PAD;
-                const uint32_t xb = (uint32_t)(x >> 32);
                 uint32_t rank = 0;
                 for (uint32_t j0 = 0; j0 < L; j0 += 32) {
-                    const uint32_t y = (j0 + lane < L) ? (uint32_t)(tmp[s0 + j0 + lane] >> 32) : 0xFFFFFFFFu;
+                    const unsigned long long y = (j0 + lane < L) ? tmp[s0 + j0 + lane] : PAD;
 #pragma unroll 8
-                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < xb;
+                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
                 }
+                slab_counts(has, x, c1, c2, c3);
                 emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
             }
         }
+        // the run's slab boundaries for decide (runs above 1023 birds are not trimmed)
+        if (lane == 0) slabs[b] = L <= 1023u ? (c1 | (c2 << 10) | (c3 << 20)) : 0xFFFFFFFFu;
     }
     flush_due(sg, lane, due, ctl);
 }
