@@ -112,7 +112,8 @@ Engine::~Engine() {
     free_graphs();
     dfree(ar_.A); dfree(ar_.B); dfree(ar_.C); dfree(ar_.D); dfree(ar_.id);
     dfree(table_d_);
-    dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
+    dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(occ2_); dfree(due_);
+    dfree(counts2_);
     dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_); dfree(slabs_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
     dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_); dfree(ndue64_);
@@ -127,11 +128,11 @@ void Engine::free_graphs() {
 }
 
 size_t Engine::bytes_for(uint32_t n) {
-    // state 2 x 68 B (two buffers) + scratch (key, arrival, occ 4 B each; tmp
-    // 8 B; due record 48 B; heading 16 B) + buckets (counts, offsets, slab
-    // boundaries 4 B each + status/4096)
+    // state 2 x 68 B (two buffers) + scratch (key, arrival, two occupied lists
+    // 4 B each; tmp 8 B; due record 48 B; heading 16 B) + buckets (two
+    // histograms, offsets, slab boundaries 4 B each + status/4096)
     const size_t b = production_buckets(n);
-    return (size_t)n * (136 + 84) + b * 12 + (b / SCAN_TILE) * 8 + 256;
+    return (size_t)n * (136 + 88) + b * 16 + (b / SCAN_TILE) * 8 + 256;
 }
 
 void Engine::set_shape(const LaunchShape& s) {
@@ -546,14 +547,15 @@ void Engine::rebuild_table(bool grid_output) {
 void Engine::ensure_scratch() {
     if (V_ > scratch_V_ || !key_) {
         const uint32_t nv = std::max<uint32_t>(V_, scratch_V_ + scratch_V_ / 2);
-        dev_bytes_ -= (size_t)scratch_V_ * 84;
+        dev_bytes_ -= (size_t)scratch_V_ * 88;
         if (sets_) dev_bytes_ -= (size_t)scratch_V_ * 32;
-        dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(due_);
+        dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(occ2_); dfree(due_);
         dfree(sfwd_); dfree(sets_);
         key_ = dalloc<uint32_t>(nv, &dev_bytes_);
         arrival_ = dalloc<uint32_t>(nv, &dev_bytes_);
         tmp_ = dalloc<unsigned long long>(nv, &dev_bytes_);
         occ_ = dalloc<uint32_t>(nv, &dev_bytes_);
+        occ2_ = dalloc<uint32_t>(nv, &dev_bytes_);
         due_ = dalloc<DueRec>(nv, &dev_bytes_);
         sfwd_ = dalloc<float4>(nv, &dev_bytes_);
         scratch_V_ = nv;
@@ -561,13 +563,15 @@ void Engine::ensure_scratch() {
     }
     if (Btot_ > scratch_B_) {
         const uint32_t nb = Btot_;
-        dev_bytes_ -= (size_t)scratch_B_ * 12 + (scratch_B_ / SCAN_TILE) * 8;
-        dfree(counts_); dfree(offsets_); dfree(status_); dfree(slabs_);
+        dev_bytes_ -= (size_t)scratch_B_ * 16 + (scratch_B_ / SCAN_TILE) * 8;
+        dfree(counts_); dfree(counts2_); dfree(offsets_); dfree(status_); dfree(slabs_);
         counts_ = dalloc<uint32_t>(nb, &dev_bytes_);
+        counts2_ = dalloc<uint32_t>(nb, &dev_bytes_);
         slabs_ = dalloc<uint32_t>(nb, &dev_bytes_);
         offsets_ = dalloc<uint32_t>((size_t)nb + 1, &dev_bytes_);
         status_ = dalloc<unsigned long long>(nb / SCAN_TILE, &dev_bytes_);
         FLK_CUDA(cudaMemsetAsync(counts_, 0, (size_t)nb * 4, stream_));
+        FLK_CUDA(cudaMemsetAsync(counts2_, 0, (size_t)nb * 4, stream_));
         FLK_CUDA(cudaMemsetAsync(status_, 0, (size_t)(nb / SCAN_TILE) * 8, stream_));
         scratch_B_ = nb;
         free_graphs();
@@ -581,32 +585,38 @@ static int pgrid(int sms, int per_sm, uint64_t items, uint64_t per_cta) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * per_sm, need));
 }
 
-void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64) {
+GridBuf Engine::grid_buf(int k) const {
+    return k ? GridBuf{counts2_, occ2_, &ctl_->occ_count[1]} : GridBuf{counts_, occ_, &ctl_->occ_count[0]};
+}
+
+void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool hash, bool fuse_next) {
     device_ahead_ = true;
     const int nfl = (int)table_h_.size();
     const int sblocks = pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256);
     const uint32_t ntiles = Btot_ / SCAN_TILE;
+    const GridBuf g = grid_buf(buf), gn = grid_buf(buf ^ 1);
     if (ev) FLK_CUDA(cudaEventRecord(ev[0], stream_));
     if (sets)  // a grid-reporting step: the reference's cell hash
-        k_hash_count<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, counts_, occ_, ctl_);
-    else
-        k_hash_count<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, counts_, occ_, ctl_);
+        k_hash_count<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
+    else if (hash)
+        k_hash_count<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
     if (sets) {
         // a step that reports its grid builds the canonical dense offsets
         // (every bucket, in bucket order) and uses them as the run starts
-        k_scan<<<ntiles, SCAN_THREADS, 0, stream_>>>(counts_, offsets_, ntiles, status_, ctl_);
+        k_scan<<<ntiles, SCAN_THREADS, 0, stream_>>>(g.counts, offsets_, ntiles, status_, ctl_);
     } else {
-        k_alloc<<<pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256), 256, 0, stream_>>>(table_d_, nfl, occ_,
-                                                                                           counts_, offsets_, ctl_);
+        k_alloc<<<pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256), 256, 0, stream_>>>(table_d_, nfl, g.occ,
+                                                                                           g.counts, offsets_,
+                                                                                           g.occ_count);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
     k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
     k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
-        table_d_, nfl, V_, ctl_, occ_, offsets_, counts_, tmp_, ar_, sfwd_, due_, slabs_);
+        table_d_, nfl, V_, ctl_, g.occ, offsets_, g.counts, g.occ_count, tmp_, ar_, sfwd_, due_, slabs_);
     if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
         k_decide_f64<<<pgrid(num_sms_, 8, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                      counts_, ar_, dec64_, ndue64_);
+                                                                      g.counts, ar_, dec64_, ndue64_);
         k_integrate_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
@@ -616,15 +626,23 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64) {
                           (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                       counts_, ar_, sfwd_, radius_table_, sets_, slabs_);
+                                                                       g.counts, ar_, sfwd_, radius_table_, sets_,
+                                                                       slabs_);
     else
         k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                        counts_, ar_, sfwd_, radius_table_, nullptr,
+                                                                        g.counts, ar_, sfwd_, radius_table_, nullptr,
                                                                         slabs_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
-    k_integrate<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, counts_, occ_, ctl_);
+    if (fuse_next && !sets)
+        k_integrate<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
+    else
+        k_integrate<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
     if (f64) k_compare_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
+}
+
+void Engine::enqueue_steps(uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i) enqueue_step(false, nullptr, false, (int)(i & 1u), i == 0, i + 1 < n);
 }
 
 void Engine::ensure_graph() {
@@ -633,7 +651,7 @@ void Engine::ensure_graph() {
     free_graphs();
     cudaGraph_t g;
     FLK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    for (uint32_t s = 0; s < chunk; ++s) enqueue_step(false);
+    enqueue_steps(chunk);
     FLK_CUDA(cudaStreamEndCapture(stream_, &g));
     cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
     cudaGraphDestroy(g);
@@ -652,7 +670,7 @@ void Engine::run(uint32_t steps) {
         device_ahead_ = true;
         for (; done + chunk <= steps; done += chunk) FLK_CUDA(cudaGraphLaunch(graph_, stream_));
     }
-    for (; done < steps; ++done) enqueue_step(false);
+    if (done < steps) enqueue_steps(steps - done);
     FLK_CUDA(cudaGetLastError());
     // host mirror of the countdown (clocks are read back on demand)
     bool finished = false;

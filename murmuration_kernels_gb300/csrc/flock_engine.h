@@ -47,18 +47,27 @@ struct Arena {
 // Step-control block in device memory: per-step counters (reset by the last
 // block of the integrate pass), the scan epoch and the device error word.
 struct StepCtl {
-    uint32_t occ_count;    // occupied buckets found this step
+    uint32_t occ_count[2];  // occupied buckets found, per grid buffer
     uint32_t due_count;    // deciding birds this step
     uint32_t scan_ticket;  // dynamic tile ids of the scan
     uint32_t epoch;        // scan status tag, advanced once per step
     uint32_t done_blocks;  // integrate's last-block detector
     uint32_t error;        // first device error (FLK_DEV_*), 0 = none
     uint32_t err_info;
-    uint32_t pad;
     unsigned long long due_total;   // cumulative deciding birds
     unsigned long long cand_total;  // cumulative candidate tests in decide
     unsigned long long pair_total;  // cumulative pairs inside 2R
     unsigned long long pad2;
+};
+
+// One of the two grid buffers: the histogram (run lengths, per bucket), the
+// occupied-bucket list and its length. A multi-step run alternates them so
+// that a step's integrate can count the next step's grid while its own is
+// cleared.
+struct GridBuf {
+    uint32_t* counts;
+    uint32_t* occ;
+    uint32_t* occ_count;
 };
 
 // One deciding bird, written by the per-bucket sort so that decide can start
@@ -170,7 +179,15 @@ private:
     void rebuild_table(bool grid_output);
     void prepare(bool grid_output);  // rebuild the table if stale or built for the other mode
     void ensure_scratch();
-    void enqueue_step(bool sets, cudaEvent_t* ev = nullptr, bool f64 = false);
+    // One step. `buf`: the grid buffer it uses; `hash`: count its grid here
+    // (otherwise the previous step's integrate did); `fuse_next`: its integrate
+    // also counts the next step's grid into the other buffer.
+    void enqueue_step(bool sets, cudaEvent_t* ev = nullptr, bool f64 = false, int buf = 0, bool hash = true,
+                      bool fuse_next = false);
+    // `n` production steps, each integrate counting the next step's grid (the
+    // first step counts its own, the last one counts none).
+    void enqueue_steps(uint32_t n);
+    GridBuf grid_buf(int k) const;
     void free_graphs();
     void ensure_graph();
     void sync_times();
@@ -204,6 +221,7 @@ private:
     DueRec* due_ = nullptr;
     float4* sfwd_ = nullptr;  // unit heading per view index (read by decide)
     uint32_t *counts_ = nullptr, *offsets_ = nullptr;
+    uint32_t *counts2_ = nullptr, *occ2_ = nullptr;  // the second grid buffer
     uint32_t* slabs_ = nullptr;  // per bucket: the run's z-slab boundaries (production steps)
     unsigned long long* status_ = nullptr;
     uint32_t* sets_ = nullptr;  // 8 per virtual bird, debug only

@@ -53,22 +53,73 @@ __global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t base, Arena s
 // ---------------------------------------------------------------------------
 // pass 1: cell key + histogram (warp-aggregated atomics)
 // ---------------------------------------------------------------------------
-// LATTICE: a production step: lattice_bucket, and the bird's 1 m z-slab in
-// its cell (0..3) rides in the top two bits of its arrival rank, so the sort
-// can order each run by slab. Otherwise the reference's cell hash, whose keys
-// a grid-reporting step returns, and slab 0 for every bird.
-// Each CTA takes 256 consecutive view indices per iteration. Bucket counts
-// use one atomic per distinct bucket of a warp; the occupied-bucket list gets
-// one atomic per CTA iteration (the first-seen buckets of all eight warps are
-// placed from a shared-memory prefix), so the single list counter is not hit
-// once per warp.
+// Counts one CTA iteration of birds into grid buffer g: a thread's bird v
+// (act) falls in bucket b, z-slab `slab`. Bucket counts use one atomic per
+// distinct bucket of a warp and give each bird its arrival rank (slab in the
+// top two bits); the occupied-bucket list gets one atomic per CTA iteration
+// (the first-seen buckets of all eight warps are placed from a shared-memory
+// prefix), so the single list counter is not hit once per warp. Called by all
+// threads of a 256-thread CTA; `it` alternates the shared slots between
+// iterations.
+__device__ __forceinline__ void count_block(bool act, uint32_t v, uint32_t b, uint32_t slab,
+                                            uint32_t* __restrict__ arrival, const GridBuf& g,
+                                            StepCtl* __restrict__ ctl, uint32_t (&s_first)[2][8], uint32_t it) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t m = __ballot_sync(FULL, act);
+    bool first = false;
+    if (act) {
+        const uint32_t peers = __match_any_sync(m, b);
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if ((int)lane == leader) old = atomicAdd(&g.counts[b], (uint32_t)__popc(peers));
+        old = __shfl_sync(m, old, leader);
+        const uint32_t rank = old + __popc(peers & lanemask_lt());
+        if (rank >= (1u << 30)) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);  // 2^30 birds in one cell
+        arrival[v] = (rank & 0x3FFFFFFFu) | (slab << 30);
+        first = rank == 0;
+    }
+    const uint32_t fm = __ballot_sync(FULL, first);
+    if (lane == 0) s_first[it][warp] = __popc(fm);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // warp 0: exclusive prefix over the eight warps + one atomic
+        const uint32_t c = lane < 8 ? s_first[it][lane] : 0u;
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, inc, o);
+            if ((int)lane >= o) inc += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, inc, 7);
+        uint32_t base = 0;
+        if (lane == 0 && total) base = atomicAdd(g.occ_count, total);
+        base = __shfl_sync(FULL, base, 0);
+        if (lane < 8) s_first[it][lane] = base + inc - c;
+    }
+    __syncthreads();
+    if (first) g.occ[s_first[it][warp] + __popc(fm & lanemask_lt())] = b;
+}
+
+// Cell of position p as its bucket (LATTICE: lattice_bucket; otherwise the
+// reference's cell hash, whose keys a grid-reporting step returns) and, in
+// production steps, its 1 m z-slab within the cell.
+template <bool LATTICE>
+__device__ __forceinline__ uint32_t bucket_slab(const float4 p, uint32_t bbase, uint32_t nb, uint32_t& slab) {
+    const int cx = cell1(p.x), cy = cell1(p.y), cz = cell1(p.z);
+    // floor(z) - 4 * floor(z / 4): z * 0.25 is exact, so this agrees with cell1
+    slab = LATTICE ? ((uint32_t)((int)floorf(p.z) - 4 * cz) & 3u) : 0u;
+    return bbase + (LATTICE ? lattice_bucket(cx, cy, cz, nb) : (cell_hash(cx, cy, cz) & (nb - 1u)));
+}
+
+// LATTICE: a production step, whose sort orders each run by z-slab (the slab
+// rides in the arrival rank); otherwise a grid-reporting step (slab 0 for
+// every bird). Each CTA takes 256 consecutive view indices per iteration.
 template <bool LATTICE>
 __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                     Arena ar, uint32_t* __restrict__ key,
-                                                    uint32_t* __restrict__ arrival, uint32_t* __restrict__ counts,
-                                                    uint32_t* __restrict__ occ, StepCtl* __restrict__ ctl) {
+                                                    uint32_t* __restrict__ arrival, GridBuf g,
+                                                    StepCtl* __restrict__ ctl) {
     __shared__ uint32_t s_first[2][8];  // per warp: first-seen buckets, then their start in occ
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t it = 0;
     for (uint32_t blk = blockIdx.x * blockDim.x; blk < V; blk += stride, it ^= 1u) {
@@ -79,48 +130,12 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
             const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
             if (__ldg(&d->remaining)) {
                 const float4 p = ar.A[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
-                const int cx = cell1(p.x), cy = cell1(p.y), cz = cell1(p.z);
-                // floor(z) - 4 * floor(z / 4): z * 0.25 is exact, so this agrees with cell1
-                if (LATTICE) slab = (uint32_t)((int)floorf(p.z) - 4 * cz) & 3u;
-                const uint32_t nb = __ldg(&d->buckets);
-                b = __ldg(&d->bbase) + (LATTICE ? lattice_bucket(cx, cy, cz, nb) : (cell_hash(cx, cy, cz) & (nb - 1u)));
+                b = bucket_slab<LATTICE>(p, __ldg(&d->bbase), __ldg(&d->buckets), slab);
                 key[v] = b;
                 act = true;
             }
         }
-        const uint32_t m = __ballot_sync(FULL, act);
-        bool first = false;
-        if (act) {
-            const uint32_t peers = __match_any_sync(m, b);
-            const int leader = __ffs(peers) - 1;
-            uint32_t old = 0;
-            if ((int)lane == leader) old = atomicAdd(&counts[b], (uint32_t)__popc(peers));
-            old = __shfl_sync(m, old, leader);
-            const uint32_t rank = old + __popc(peers & lanemask_lt());
-            if (rank >= (1u << 30)) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);  // 2^30 birds in one cell
-            arrival[v] = (rank & 0x3FFFFFFFu) | (slab << 30);
-            first = rank == 0;
-        }
-        const uint32_t fm = __ballot_sync(FULL, first);
-        if (lane == 0) s_first[it][warp] = __popc(fm);
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            // warp 0: exclusive prefix over the eight warps + one atomic
-            const uint32_t c = lane < 8 ? s_first[it][lane] : 0u;
-            uint32_t inc = c;
-#pragma unroll
-            for (int o = 1; o < 8; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, inc, o);
-                if ((int)lane >= o) inc += y;
-            }
-            const uint32_t total = __shfl_sync(FULL, inc, 7);
-            uint32_t base = 0;
-            if (lane == 0 && total) base = atomicAdd(&ctl->occ_count, total);
-            base = __shfl_sync(FULL, base, 0);
-            if (lane < 8) s_first[it][lane] = base + inc - c;
-        }
-        __syncthreads();
-        if (first) occ[s_first[it][warp] + __popc(fm & lanemask_lt())] = b;
+        count_block(act, v, b, slab, arrival, g, ctl, s_first, it);
     }
 }
 
@@ -241,9 +256,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
 // stays in counts[b] until integrate clears it.
 __global__ void __launch_bounds__(256) k_alloc(FlockDesc* __restrict__ fl, int nfl, const uint32_t* __restrict__ occ,
                                                const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
-                                               StepCtl* __restrict__ ctl) {
+                                               const uint32_t* __restrict__ occ_count) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
+    const uint32_t nocc = *(volatile const uint32_t*)occ_count;
     for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nocc; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0 + lane;
         const bool act = i < nocc;
@@ -436,6 +451,7 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
                                                  const uint32_t* __restrict__ counts,
+                                                 const uint32_t* __restrict__ occ_count,
                                                  const unsigned long long* __restrict__ tmp, Arena ar,
                                                  float4* __restrict__ sfwd, DueRec* __restrict__ due,
                                                  uint32_t* __restrict__ slabs) {
@@ -444,7 +460,7 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
+    const uint32_t nocc = *(volatile const uint32_t*)occ_count;
     DueStage sg{s_due[(threadIdx.x >> 5) & 7], 0u};
     // each warp takes a contiguous range of occupied buckets (neighbouring
     // cells), so a batch of staged records stays spatially close for decide

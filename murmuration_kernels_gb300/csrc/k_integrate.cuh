@@ -3,6 +3,7 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "k_grid.cuh"
 
 namespace flk {
 
@@ -10,53 +11,76 @@ namespace flk {
 // pass 6: integrate (model.rs:149-176) + end-of-step bookkeeping
 // ---------------------------------------------------------------------------
 // Works on the buffer the sort pass wrote (parity ^ 1); the last block makes
-// that buffer current.
+// that buffer current. Clears this step's histogram entries (grid buffer cur).
+// FUSE (production runs of several steps): also counts the next step's grid
+// from the new positions into grid buffer nxt (key, arrival rank, histogram,
+// occupied list) for every flock that steps again, so the next step needs no
+// separate hash pass; the counting is count_block, as in k_hash_count.
+template <bool FUSE>
 __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
-                                                   uint32_t* __restrict__ counts, const uint32_t* __restrict__ occ,
-                                                   StepCtl* __restrict__ ctl) {
-    // the histogram's occupied entries go back to zero for the next step
-    const uint32_t nocc = *(volatile uint32_t*)&ctl->occ_count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nocc; i += gridDim.x * blockDim.x) counts[occ[i]] = 0;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
-        if (!d->remaining) continue;
-        float4* __restrict__ A = ar.A;
-        float4* __restrict__ B = ar.B;
-        const float4* __restrict__ C = ar.C;
-        const uint32_t st = v + view_shift(d->sbase, d->vbase, d->parity ^ 1u, ar.cap);
-        const float4 a = A[st];
-        const float4 b = B[st];
-        const float4 c = C[st];
-        f3 vel = xyz(b);
-        const f3 steering = xyz(c);
-        const float roll = a.w;
+                                                   GridBuf cur, GridBuf nxt, uint32_t* __restrict__ key,
+                                                   uint32_t* __restrict__ arrival, StepCtl* __restrict__ ctl) {
+    __shared__ uint32_t s_first[2][8];
+    // the histogram's occupied entries go back to zero for the step after next
+    const uint32_t nocc = *(volatile const uint32_t*)cur.occ_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nocc; i += gridDim.x * blockDim.x)
+        cur.counts[cur.occ[i]] = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t it = 0;
+    for (uint32_t blk = blockIdx.x * blockDim.x; blk < V; blk += stride, it ^= 1u) {
+        const uint32_t v = blk + threadIdx.x;
+        bool act = false;
+        uint32_t b = 0, slab = 0;
+        if (v < V) {
+            const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
+            const uint32_t rem = d->remaining;
+            if (rem) {
+                float4* __restrict__ A = ar.A;
+                float4* __restrict__ B = ar.B;
+                const float4* __restrict__ C = ar.C;
+                const uint32_t st = v + view_shift(d->sbase, d->vbase, d->parity ^ 1u, ar.cap);
+                const float4 a = A[st];
+                const float4 bv = B[st];
+                const float4 c = C[st];
+                f3 vel = xyz(bv);
+                const f3 steering = xyz(c);
+                const float roll = a.w;
 
-        const f3 fw = forward(vel);
-        const f3 side = side_of(fw);
-        const float speed = fmaxf(len(vel), 1e-6f);
-        const float a_lat = __fdiv_rn(dot(steering, side), MASS);
-        const float target = clampf(atanf(__fdiv_rn(a_lat, G)), -MAX_BANK, MAX_BANK);
-        const float rate = clampf(__fdiv_rn(__fsub_rn(target, roll), TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
-        const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
+                const f3 fw = forward(vel);
+                const f3 side = side_of(fw);
+                const float speed = fmaxf(len(vel), 1e-6f);
+                const float a_lat = __fdiv_rn(dot(steering, side), MASS);
+                const float target = clampf(atanf(__fdiv_rn(a_lat, G)), -MAX_BANK, MAX_BANK);
+                const float rate = clampf(__fdiv_rn(__fsub_rn(target, roll), TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
+                const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
 
-        const f3 up = body_up(fw, beta);
-        const float cos_beta = fmaxf(cosf(beta), 0.2f);
-        const float sr = __fdiv_rn(speed, V0);
-        const float sr2 = __fmul_rn(sr, sr);
-        const float lift = __fdiv_rn(__fmul_rn(sr2, L0), cos_beta);
-        const float drag = __fmul_rn(sr2, D0);
-        const f3 flight = sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mul(mul(mk(0.f, 0.f, 1.f), MASS), G));
-        const f3 control = sub(steering, mul(side, dot(steering, side)));
-        vel = add(vel, mul(dvs(add(control, flight), MASS), DT));
-        const float sp = len(vel);
-        if (sp > V_MAX) {
-            vel = mul(vel, __fdiv_rn(V_MAX, sp));
-        } else if (sp < V_MIN && sp > 1e-6f) {
-            vel = mul(vel, __fdiv_rn(V_MIN, sp));
+                const f3 up = body_up(fw, beta);
+                const float cos_beta = fmaxf(cosf(beta), 0.2f);
+                const float sr = __fdiv_rn(speed, V0);
+                const float sr2 = __fmul_rn(sr, sr);
+                const float lift = __fdiv_rn(__fmul_rn(sr2, L0), cos_beta);
+                const float drag = __fmul_rn(sr2, D0);
+                const f3 flight =
+                    sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mul(mul(mk(0.f, 0.f, 1.f), MASS), G));
+                const f3 control = sub(steering, mul(side, dot(steering, side)));
+                vel = add(vel, mul(dvs(add(control, flight), MASS), DT));
+                const float sp = len(vel);
+                if (sp > V_MAX) {
+                    vel = mul(vel, __fdiv_rn(V_MAX, sp));
+                } else if (sp < V_MIN && sp > 1e-6f) {
+                    vel = mul(vel, __fdiv_rn(V_MIN, sp));
+                }
+                const f3 pos = add(xyz(a), mul(vel, DT));
+                A[st] = make_float4(pos.x, pos.y, pos.z, beta);
+                B[st] = make_float4(vel.x, vel.y, vel.z, rate);
+                if (FUSE && rem >= 2) {  // this flock steps again: its bird's cell for the next step
+                    b = bucket_slab<true>(make_float4(pos.x, pos.y, pos.z, 0.f), d->bbase, d->buckets, slab);
+                    key[v] = b;
+                    act = true;
+                }
+            }
         }
-        const f3 pos = add(xyz(a), mul(vel, DT));
-        A[st] = make_float4(pos.x, pos.y, pos.z, beta);
-        B[st] = make_float4(vel.x, vel.y, vel.z, rate);
+        if (FUSE) count_block(act, v, b, slab, arrival, nxt, ctl, s_first, it);
     }
     // the last block to finish advances every active flock and resets the step counters
     __shared__ bool s_last;
@@ -77,7 +101,7 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
             }
         }
         if (threadIdx.x == 0) {
-            ctl->occ_count = 0;
+            *cur.occ_count = 0;
             ctl->due_count = 0;
             ctl->scan_ticket = 0;
             ctl->epoch = ctl->epoch + 1;
