@@ -114,6 +114,12 @@ int flk_batch_step_debug(flk_batch* b, const int32_t* ids, uint32_t count, uint3
                          uint32_t* sorted, uint32_t* sets);
 /* Launch shape: CTAs per SM of the streaming passes and decide, decide CTA
  * size, steps per captured graph. Zero keeps the current value. */
+/* flk_step_f64 for the listed flocks (one step each, the others idle):
+ * `out64` (optional) receives each listed flock's FP64 post-step state
+ * (n_f*15 doubles, bird order) concatenated in the order of `ids`; `reports`
+ * (optional, 4 doubles per id) each flock's own error report, as flk_step_f64
+ * gives it. A duplicated id is FLK_ERR_ARG. */
+int flk_batch_step_f64(flk_batch* b, const int32_t* ids, uint32_t count, double* out64, double* reports);
 int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t decide_threads, int32_t graph_chunk);
 int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
 /* Times `steps` graph-launched steps on the batch's stream with CUDA events. */
@@ -159,6 +165,12 @@ int flk_pool_submit_file(flk_pool* p, const char* path, uint32_t steps, float* o
  * continues the flock exactly. No counterpart in the reference. */
 int flk_pool_snapshot(flk_pool* p, uint64_t ticket, float* words, float* time, uint32_t* steps_done,
                       const char* path);
+/* Error report of a request's next step: takes the request's current state
+ * as flk_pool_snapshot does (steps_done optional), then runs flk_step_f64 on
+ * a private copy on the pool's device. The served flock is not advanced;
+ * `out64` (optional, n*15) and `report` (optional, 4) as in flk_step_f64.
+ * The copy's device memory is outside the pool's budget. */
+int flk_pool_error_report(flk_pool* p, uint64_t ticket, double* out64, double* report, uint32_t* steps_done);
 /* *state: 0 queued, 1 resident, 2 done, negative FLK_ERR_* on failure. */
 int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state);
 /* Blocks until done; *latency_ms = completion - submission (host clock). */

@@ -85,6 +85,7 @@ _SIGS = {
     "flk_batch_step_each": (C.c_int, [_P, _PI, _PU, C.c_uint32]),
     "flk_batch_read": (C.c_int, [_P, C.c_int32, _PF, _PF]),
     "flk_batch_step_debug": (C.c_int, [_P, _PI, C.c_uint32, _PU, _PU, _PU, _PU]),
+    "flk_batch_step_f64": (C.c_int, [_P, _PI, C.c_uint32, _PD, _PD]),
     "flk_batch_tune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "flk_batch_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
     "flk_batch_time_steps": (C.c_int, [_P, C.c_uint32, _PD]),
@@ -94,6 +95,7 @@ _SIGS = {
     "flk_pool_submit": (C.c_int, [_P, C.c_uint32, C.c_float, _PF, C.c_uint32, _PF, _PF, _PU64]),
     "flk_pool_submit_file": (C.c_int, [_P, C.c_char_p, C.c_uint32, _PF, C.c_uint32, _PF, _PU64, _PU]),
     "flk_pool_snapshot": (C.c_int, [_P, C.c_uint64, _PF, _PF, _PU, C.c_char_p]),
+    "flk_pool_error_report": (C.c_int, [_P, C.c_uint64, _PD, _PD, _PU]),
     "flk_pool_poll": (C.c_int, [_P, C.c_uint64, _PI]),
     "flk_pool_wait": (C.c_int, [_P, C.c_uint64, _PD]),
     "flk_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
@@ -285,8 +287,7 @@ class Flock:
         out = np.empty((self.n, WORDS), dtype=np.float64)
         rep = np.zeros(4, dtype=np.float64)
         _check(lib().flk_step_f64(self._h, out.ctypes.data_as(_PD), rep.ctypes.data_as(_PD)))
-        return out, {"max_rel_pos": float(rep[0]), "max_rel_vel": float(rep[1]),
-                     "neighbour_mismatches": int(rep[2]), "deciding": int(rep[3])}
+        return out, _f64_report(rep)
 
     def counters(self) -> tuple[int, int, int]:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
@@ -318,6 +319,11 @@ class Flock:
 
 
 # ---- batched -----------------------------------------------------------------
+def _f64_report(rep: np.ndarray) -> dict[str, float]:
+    return {"max_rel_pos": float(rep[0]), "max_rel_vel": float(rep[1]),
+            "neighbour_mismatches": int(rep[2]), "deciding": int(rep[3])}
+
+
 class Batch:
     """Many independent flocks advanced together (one launch per pass)."""
 
@@ -368,6 +374,21 @@ class Batch:
             k += n
             o += b + 1
         return out
+
+    def step_f64(self, ids: Sequence[int]) -> list[tuple[np.ndarray, dict[str, float]]]:
+        """One step of each listed flock with its FP64 evaluation (as
+        Flock.step_f64): per id (FP64 post-step state [n, 15], error report)."""
+        a = np.asarray(ids, dtype=np.int32)
+        ns = [self.sizes[i] for i in ids]
+        out = np.empty((sum(ns), WORDS), dtype=np.float64)
+        rep = np.zeros((len(a), 4), dtype=np.float64)
+        _check(lib().flk_batch_step_f64(self._h, a.ctypes.data_as(_PI), len(a), out.ctypes.data_as(_PD),
+                                        rep.ctypes.data_as(_PD)))
+        res, k = [], 0
+        for i, n in enumerate(ns):
+            res.append((out[k:k + n], _f64_report(rep[i])))
+            k += n
+        return res
 
     def tune(self, stream_bps: int = 0, decide_bps: int = 0, decide_threads: int = 0, graph_chunk: int = 0) -> None:
         _check(lib().flk_batch_tune(self._h, stream_bps, decide_bps, decide_threads, graph_chunk))
@@ -449,6 +470,20 @@ class Pool:
         _check(lib().flk_pool_snapshot(self._h, ticket, _fptr(w), _fptr(t), C.byref(k),
                                        path.encode() if path else None))
         return float(t[0]), w, k.value
+
+    def error_report(self, ticket: int) -> tuple[np.ndarray, dict[str, float], int]:
+        """The FP64 evaluation of the request's next step, run on a copy of its
+        current state (the served flock is not advanced): (FP64 post-step
+        state [n, 15], error report, steps done at the snapshot)."""
+        if ticket not in self._keep:
+            raise ValueError("error_report: unknown ticket, or its result was already collected by wait()")
+        n = self._keep[ticket][1].shape[0]
+        out = np.empty((n, WORDS), dtype=np.float64)
+        rep = np.zeros(4, dtype=np.float64)
+        k = C.c_uint32()
+        _check(lib().flk_pool_error_report(self._h, ticket, out.ctypes.data_as(_PD), rep.ctypes.data_as(_PD),
+                                           C.byref(k)))
+        return out, _f64_report(rep), k.value
 
     def poll(self, ticket: int) -> int:
         s = C.c_int32()

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -202,11 +203,11 @@ extern "C" int flk_step_f64(flk_flock* f, double* out64, double* report) {
     return guarded([&] {
         f->eng->set_remaining({f->id}, {1u});
         std::vector<std::vector<double>> out;
-        double rep[4];
-        f->eng->step_f64(&out, rep);
+        std::vector<std::array<double, 4>> rep;
+        f->eng->step_f64(&out, &rep);
         if (out.size() != 1) return fail(FLK_ERR_ARG, "flk_step_f64: flock not stepped");
         if (out64 && !out[0].empty()) std::memcpy(out64, out[0].data(), out[0].size() * 8);
-        if (report) std::memcpy(report, rep, sizeof rep);
+        if (report) std::memcpy(report, rep[0].data(), 4 * sizeof(double));
         return check_device(*f->eng);
     });
 }
@@ -331,6 +332,34 @@ extern "C" int flk_batch_step_debug(flk_batch* b, const int32_t* ids, uint32_t c
             oo += g.offsets.size();
             so += g.sorted.size();
             zo += g.sets.size();
+        }
+        return check_device(*b->eng);
+    });
+}
+
+extern "C" int flk_batch_step_f64(flk_batch* b, const int32_t* ids, uint32_t count, double* out64,
+                                  double* reports) {
+    if (!b || (count && !ids)) return fail(FLK_ERR_ARG, "flk_batch_step_f64: null pointer");
+    return guarded([&] {
+        std::vector<int> v(ids, ids + count);
+        for (int id : v)
+            if (!b->eng->has_flock(id)) return fail(FLK_ERR_ID, "flk_batch_step_f64: unknown flock id");
+        std::vector<int> sorted_ids = v;
+        std::sort(sorted_ids.begin(), sorted_ids.end());
+        if (std::adjacent_find(sorted_ids.begin(), sorted_ids.end()) != sorted_ids.end())
+            return fail(FLK_ERR_ARG, "flk_batch_step_f64: a flock id is listed twice");
+        b->eng->set_remaining(v, std::vector<uint32_t>(count, 1u));
+        std::vector<std::vector<double>> out;
+        std::vector<std::array<double, 4>> rep;
+        b->eng->step_f64(&out, &rep);
+        // the engine reports the stepped flocks in slot (= id) order
+        if (out.size() != count) return fail(FLK_ERR_ARG, "flk_batch_step_f64: a flock was not stepped");
+        size_t o = 0;
+        for (uint32_t i = 0; i < count; ++i) {
+            const size_t k = (size_t)(std::lower_bound(sorted_ids.begin(), sorted_ids.end(), v[i]) - sorted_ids.begin());
+            if (out64 && !out[k].empty()) std::memcpy(out64 + o, out[k].data(), out[k].size() * 8);
+            o += out[k].size();
+            if (reports) std::memcpy(reports + 4 * (size_t)i, rep[k].data(), 4 * sizeof(double));
         }
         return check_device(*b->eng);
     });
@@ -737,6 +766,31 @@ extern "C" int flk_pool_snapshot(flk_pool* p, uint64_t ticket, float* words, flo
     if (time) *time = t;
     if (steps_done) *steps_done = k;
     return path ? write_flk(path, t, words, r->n) : FLK_OK;
+}
+
+extern "C" int flk_pool_error_report(flk_pool* p, uint64_t ticket, double* out64, double* report,
+                                     uint32_t* steps_done) {
+    if (!p) return fail(FLK_ERR_ARG, "flk_pool_error_report: null handle");
+    uint32_t n = 0;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        auto it = p->reqs.find(ticket);
+        if (it == p->reqs.end()) return fail(FLK_ERR_ID, "flk_pool_error_report: unknown ticket");
+        n = it->second->n;
+    }
+    std::vector<float> words((size_t)n * flk::WORDS);
+    float t = 0.f;
+    int rc = flk_pool_snapshot(p, ticket, words.data(), &t, steps_done, nullptr);
+    if (rc) return rc;
+    // the evaluation runs on a private copy on the pool's device, beside the
+    // worker's stream: the served flock is neither paused beyond the
+    // snapshot's chunk boundary nor advanced
+    flk_flock* f = nullptr;
+    rc = flk_open_host(p->eng->device(), n, t, words.data(), &f);
+    if (rc) return rc;
+    rc = flk_step_f64(f, out64, report);
+    flk_close(f);
+    return rc;
 }
 
 extern "C" int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state) {

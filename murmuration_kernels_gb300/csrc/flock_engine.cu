@@ -116,7 +116,7 @@ Engine::~Engine() {
     dfree(counts2_);
     dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_); dfree(slabs_);
     dfree(ctl_); dfree(radius_table_); dfree(staging_);
-    dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_); dfree(ndue64_);
+    dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_);
     if (copy_) cudaStreamDestroy(copy_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -616,7 +616,7 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
         table_d_, nfl, V_, ctl_, g.occ, offsets_, g.counts, g.occ_count, tmp_, ar_, sfwd_, due_, slabs_);
     if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
         k_decide_f64<<<pgrid(num_sms_, 8, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                      g.counts, ar_, dec64_, ndue64_);
+                                                                      g.counts, ar_, dec64_, err64_);
         k_integrate_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
@@ -768,11 +768,11 @@ void Engine::step_debug(std::vector<GridDebug>* out) {
     table_dirty_ = true;
 }
 
-void Engine::step_f64(std::vector<std::vector<double>>* out, double report[4]) {
+void Engine::step_f64(std::vector<std::vector<double>>* out, std::vector<std::array<double, 4>>* report) {
     FLK_CUDA(cudaSetDevice(device_));
     prepare(false);  // production buckets: the FP64 passes use the lattice index
     out->clear();
-    for (int k = 0; k < 4; ++k) report[k] = 0.0;
+    report->clear();
     if (table_h_.empty()) return;
     if (V_ > f64_V_ || !dec64_) {
         dfree(dec64_);
@@ -781,25 +781,23 @@ void Engine::step_f64(std::vector<std::vector<double>>* out, double report[4]) {
         out64_ = dalloc<double>((size_t)V_ * 15, &dev_bytes_);
         f64_V_ = V_;
     }
-    if (table_h_.size() > active_cap_ || !active_) {
+    const size_t nfl = table_h_.size();
+    if (nfl > active_cap_ || !active_) {
         dfree(active_);
-        active_cap_ = (uint32_t)table_h_.size();
+        dfree(err64_);
+        active_cap_ = (uint32_t)nfl;
         active_ = dalloc<uint8_t>(active_cap_, &dev_bytes_);
+        err64_ = dalloc<uint32_t>((size_t)active_cap_ * 4, &dev_bytes_);
     }
-    if (!err64_) err64_ = dalloc<uint32_t>(4, &dev_bytes_);
-    if (!ndue64_) ndue64_ = dalloc<unsigned long long>(1, &dev_bytes_);
     const std::vector<FlockDesc> before = table_h_;
-    std::vector<uint8_t> act(before.size());
-    for (size_t k = 0; k < before.size(); ++k) act[k] = before[k].remaining > 0;
-    FLK_CUDA(cudaMemcpyAsync(active_, act.data(), act.size(), cudaMemcpyHostToDevice, stream_));
-    FLK_CUDA(cudaMemsetAsync(err64_, 0, 16, stream_));
-    FLK_CUDA(cudaMemsetAsync(ndue64_, 0, 8, stream_));
+    std::vector<uint8_t> act(nfl);
+    for (size_t k = 0; k < nfl; ++k) act[k] = before[k].remaining > 0;
+    FLK_CUDA(cudaMemcpyAsync(active_, act.data(), nfl, cudaMemcpyHostToDevice, stream_));
+    FLK_CUDA(cudaMemsetAsync(err64_, 0, nfl * 16, stream_));
     enqueue_step(false, nullptr, true);
     FLK_CUDA(cudaGetLastError());
-    uint32_t err[4];
-    unsigned long long nd = 0;
-    FLK_CUDA(cudaMemcpyAsync(err, err64_, 16, cudaMemcpyDeviceToHost, stream_));
-    FLK_CUDA(cudaMemcpyAsync(&nd, ndue64_, 8, cudaMemcpyDeviceToHost, stream_));
+    std::vector<uint32_t> err(nfl * 4);
+    FLK_CUDA(cudaMemcpyAsync(err.data(), err64_, nfl * 16, cudaMemcpyDeviceToHost, stream_));
     std::vector<double> o64((size_t)V_ * 15);
     FLK_CUDA(cudaMemcpyAsync(o64.data(), out64_, o64.size() * 8, cudaMemcpyDeviceToHost, stream_));
     std::vector<uint32_t> ids[2];
@@ -810,16 +808,15 @@ void Engine::step_f64(std::vector<std::vector<double>>* out, double report[4]) {
                                      cudaMemcpyDeviceToHost, stream_));
     }
     FLK_CUDA(cudaStreamSynchronize(stream_));
-    float ep, ev;
-    std::memcpy(&ep, &err[0], 4);
-    std::memcpy(&ev, &err[1], 4);
-    report[0] = ep;
-    report[1] = ev;
-    report[2] = err[2];
-    report[3] = (double)nd;
-    for (const FlockDesc& d : before) {
+    for (size_t f = 0; f < nfl; ++f) {
+        const FlockDesc& d = before[f];
         std::vector<double> w;
+        std::array<double, 4> r{0.0, 0.0, 0.0, 0.0};
         if (d.remaining) {
+            float ep, ev;
+            std::memcpy(&ep, &err[4 * f], 4);
+            std::memcpy(&ev, &err[4 * f + 1], 4);
+            r = {ep, ev, (double)err[4 * f + 2], (double)err[4 * f + 3]};
             // view index vbase + i sits in slot sbase + i of the copy the step wrote
             const std::vector<uint32_t>& nid = ids[(d.parity & 1u) ^ 1u];
             w.resize((size_t)d.n * 15);
@@ -830,6 +827,7 @@ void Engine::step_f64(std::vector<std::vector<double>>* out, double report[4]) {
             }
         }
         out->push_back(std::move(w));
+        report->push_back(r);
     }
 }
 

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -147,11 +148,12 @@ public:
     // One eager step that also returns every flock's grid and set summaries.
     void step_debug(std::vector<GridDebug>* out);
     // One production step of every active flock that also evaluates the same
-    // step in FP64 from the same input state. out[k] (per table flock, bird
-    // order, n*15) receives the FP64 post-step state; report = {max relative
-    // position error, max relative velocity error, neighbour-count
-    // mismatches, deciding birds} of the f32 step against it.
-    void step_f64(std::vector<std::vector<double>>* out, double report[4]);
+    // step in FP64 from the same input state. Per table flock k (empty for
+    // flocks that did not step): out[k] (bird order, n*15) receives the FP64
+    // post-step state, report[k] = {max relative position error, max
+    // relative velocity error, neighbour-count mismatches, deciding birds}
+    // of its f32 step against it.
+    void step_f64(std::vector<std::vector<double>>* out, std::vector<std::array<double, 4>>* report);
     void sync();
     uint32_t check_device_error();  // returns and clears the device error word
 
@@ -235,8 +237,7 @@ private:
     uint32_t f64_V_ = 0;
     uint8_t* active_ = nullptr;
     uint32_t active_cap_ = 0;
-    uint32_t* err64_ = nullptr;
-    unsigned long long* ndue64_ = nullptr;
+    uint32_t* err64_ = nullptr;  // 4 words per table flock
 
     cudaGraphExec_t graph_ = nullptr;
     uint32_t graph_steps_ = 0;

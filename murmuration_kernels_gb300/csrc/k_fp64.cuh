@@ -72,12 +72,13 @@ __device__ __forceinline__ double wsum(double v) {
 // One warp per deciding bird. Candidates: every distinct bucket of the cells a
 // conservative 2r box touches (the f32 step's reach bounds every FP64 pair as
 // well), or the flock's whole range when the box is wide. dec[view] receives
-// steering xyz, radius, neighbour count, centrality, next decision.
+// steering xyz, radius, neighbour count, centrality, next decision; err[4f + 3]
+// counts flock f's deciding birds.
 __global__ void __launch_bounds__(256) k_decide_f64(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                     StepCtl* __restrict__ ctl, const DueRec* __restrict__ due,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ counts, Arena ar,
-                                                    double* __restrict__ dec, unsigned long long* __restrict__ ndue) {
+                                                    double* __restrict__ dec, uint32_t* __restrict__ err) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(256) k_decide_f64(const FlockDesc* __restrict_
             o[4] = n_all;
             o[5] = cen;
             o[6] = (double)d_me.x + (double)DU;
-            atomicAdd(ndue, 1ull);
+            atomicAdd(&err[4 * find_flock_v(fl, nfl, k) + 3], 1u);
         }
     }
 }
@@ -234,38 +235,46 @@ __global__ void __launch_bounds__(256) k_integrate_f64(const FlockDesc* __restri
 
 // After the f32 step: per bird the relative error of position and velocity
 // (||f32 - f64|| / max(||f64||, 1e-6)) and whether the neighbour counts
-// differ. err[0], err[1]: maxima as float bits; err[2]: mismatches.
-// active[f]: flock f of the table was stepped (its parity is flipped by now).
+// differ, reduced per flock f of the table: err[4f], err[4f + 1] maxima as
+// float bits, err[4f + 2] mismatches. active[f]: flock f was stepped (its
+// parity is flipped by now). The loop is warp-uniform; lanes of one flock
+// reduce together (match_any) and their first lane updates the flock's words.
 __global__ void __launch_bounds__(256) k_compare_f64(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                      Arena ar, const uint8_t* __restrict__ active,
                                                      const double* __restrict__ out, uint32_t* __restrict__ err) {
-    float mp = 0.f, mv = 0.f;
-    uint32_t mism = 0;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int f = find_flock_v(fl, nfl, v);
-        if (!active[f]) continue;
-        const FlockDesc* d = &fl[f];
-        const uint32_t st = v + view_shift(d->sbase, d->vbase, d->parity, ar.cap);
-        const double* w = out + (size_t)v * 15;
-        const float4 a = ar.A[st], b = ar.B[st];
-        const float nb = ar.D[st].y;
-        const d3 dp = dsub(dxyz(a), dmk(w[0], w[1], w[2])), dv = dsub(dxyz(b), dmk(w[3], w[4], w[5]));
-        mp = fmaxf(mp, (float)(dlen(dp) / fmax(dlen(dmk(w[0], w[1], w[2])), 1e-6)));
-        mv = fmaxf(mv, (float)(dlen(dv) / fmax(dlen(dmk(w[3], w[4], w[5])), 1e-6)));
-        mism += (double)__float_as_uint(nb) != w[13];
-    }
-    mp = fmaxf(mp, __shfl_xor_sync(FULL, mp, 16));
-    mv = fmaxf(mv, __shfl_xor_sync(FULL, mv, 16));
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) {
-        mp = fmaxf(mp, __shfl_xor_sync(FULL, mp, o));
-        mv = fmaxf(mv, __shfl_xor_sync(FULL, mv, o));
-    }
-    mism = __reduce_add_sync(FULL, mism);
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&err[0], __float_as_uint(mp));  // non-negative floats order as their bits
-        atomicMax(&err[1], __float_as_uint(mv));
-        if (mism) atomicAdd(&err[2], mism);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t blk = blockIdx.x * blockDim.x; blk < V; blk += stride) {
+        const uint32_t v = blk + threadIdx.x;
+        int f = -1;
+        float mp = 0.f, mv = 0.f;
+        uint32_t mism = 0;
+        if (v < V) {
+            f = find_flock_v(fl, nfl, v);
+            if (active[f]) {
+                const FlockDesc* d = &fl[f];
+                const uint32_t st = v + view_shift(d->sbase, d->vbase, d->parity, ar.cap);
+                const double* w = out + (size_t)v * 15;
+                const float4 a = ar.A[st], b = ar.B[st];
+                const float nb = ar.D[st].y;
+                const d3 dp = dsub(dxyz(a), dmk(w[0], w[1], w[2])), dv = dsub(dxyz(b), dmk(w[3], w[4], w[5]));
+                mp = (float)(dlen(dp) / fmax(dlen(dmk(w[0], w[1], w[2])), 1e-6));
+                mv = (float)(dlen(dv) / fmax(dlen(dmk(w[3], w[4], w[5])), 1e-6));
+                mism = (double)__float_as_uint(nb) != w[13];
+            } else {
+                f = -1;
+            }
+        }
+        const uint32_t peers = __match_any_sync(FULL, f);
+        // non-negative floats order as their bits
+        const uint32_t bp = __reduce_max_sync(peers, __float_as_uint(mp));
+        const uint32_t bv = __reduce_max_sync(peers, __float_as_uint(mv));
+        const uint32_t bm = __reduce_add_sync(peers, mism);
+        if (f >= 0 && (int)lane == __ffs(peers) - 1) {
+            atomicMax(&err[4 * f], bp);
+            atomicMax(&err[4 * f + 1], bv);
+            if (bm) atomicAdd(&err[4 * f + 2], bm);
+        }
     }
 }
 

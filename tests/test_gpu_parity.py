@@ -578,3 +578,63 @@ def test_fp64_step_matches_the_oracle_fp64_twin(native, oracle, n, seed, settle)
     assert 0 < rep["max_rel_pos"] <= REL_TOL and rep["max_rel_vel"] <= REL_TOL
     assert rep["deciding"] == int((np.float32(np.float32(t0) + np.float32(0.005)) >= w[:, 12]).sum())
     assert rep["neighbour_mismatches"] == int((g[:, 13].view(np.uint32) != d[:, 13]).sum())
+
+
+def test_batch_fp64_reports_each_flock_as_its_plain_handle(native, oracle):
+    """flk_batch_step_f64: each listed flock gets the FP64 state and the error
+    report its own plain handle gives from the same input, in the caller's id
+    order; listed flocks advance exactly one step, the others stay idle."""
+    ws = [oracle.scatter(2000, 1), oracle.scatter(7000, 4), oracle.scatter(4500, 9)]
+    b = native.Batch()
+    ids = [b.add(w) for w in ws]
+    pick = [ids[2], ids[0]]
+    res = b.step_f64(pick)
+    for fid, (out, rep) in zip(pick, res):
+        w = ws[ids.index(fid)]
+        f = native.Flock(w)
+        o1, r1 = f.step_f64()
+        t1, g1 = f.read()
+        f.close()
+        assert out.tobytes() == o1.tobytes() and rep == r1
+        assert 0 < rep["max_rel_pos"] <= REL_TOL and rep["deciding"] > 0
+        tb, gb = b.read(fid)
+        assert tb == t1 and gb.tobytes() == g1.tobytes()
+    t_idle, w_idle = b.read(ids[1])
+    assert t_idle == 0.0 and w_idle.tobytes() == ws[1].tobytes()
+    with pytest.raises(native.FlockError):
+        b.step_f64([ids[0], ids[0]])
+    b.close()
+
+
+def test_pool_error_report_evaluates_a_live_flock_without_advancing_it(native):
+    """flk_pool_error_report: the report of a resident request equals the
+    plain handle's flk_step_f64 after the reported number of steps; the
+    request still ends exactly as an uninterrupted run. A queued request
+    reports on its input."""
+    a = native.generate(6000, 81)
+    with native.Pool(budget_bytes=native.bytes_for(6000), chunk_steps=4) as pool:
+        ta = pool.submit(a, 2000)  # long enough that the second request is still queued below
+        tq = pool.submit(native.generate(3000, 82), 5)
+        assert pool.poll(tq) == 0
+        oq, rq, kq = pool.error_report(tq)
+        while pool.poll(ta) == 0:
+            pass
+        out, rep, k = pool.error_report(ta)
+        t1, w1, _ = pool.wait(ta)
+        pool.wait(tq)
+    assert 0 <= k <= 2000 and kq == 0
+    p = native.Flock(a)
+    p.step(k)
+    o2, r2 = p.step_f64()
+    p.close()
+    assert out.tobytes() == o2.tobytes() and rep == r2
+    assert rep["max_rel_pos"] <= REL_TOL and rep["max_rel_vel"] <= REL_TOL
+    q = native.Flock(native.generate(3000, 82))
+    oq2, rq2 = q.step_f64()
+    q.close()
+    assert oq.tobytes() == oq2.tobytes() and rq == rq2
+    p = native.Flock(a)
+    p.step(2000)
+    tp, wp = p.read()
+    p.close()
+    assert tp == t1 and wp.tobytes() == w1.tobytes()
