@@ -7,12 +7,13 @@
 //
 //   k_hash_count  cell key per bird + bucket histogram with warp-aggregated
 //                 atomics (__match_any_sync); records each bird's arrival rank
-//                 and appends first-seen buckets to an occupied-bucket list
-//                 (one atomic per CTA iteration). Production steps bucket
-//                 cells by a lattice index, grid-reporting steps by the
-//                 reference's hash.
-//   k_alloc       production steps: each occupied bucket's run start from a
-//                 per-flock cursor (one atomic per warp).
+//                 and, in grid-reporting steps, appends first-seen buckets to
+//                 an occupied-bucket list (one atomic per CTA iteration).
+//                 Production steps bucket cells by a lattice index,
+//                 grid-reporting steps by the reference's hash.
+//   k_place       production steps: lists the occupied buckets in lattice
+//                 order from the histogram and gives each its run start from
+//                 a per-flock cursor (one atomic per warp).
 //   k_scan        grid-reporting steps: single-pass decoupled look-back
 //                 exclusive scan of the histogram into the canonical dense
 //                 offsets (buckets+1 entries). Bounded waits.
@@ -143,6 +144,21 @@ void Engine::set_shape(const LaunchShape& s) {
                                   (int)(w * decide_smem_per_warp<false>())));
     FLK_CUDA(cudaFuncSetAttribute(k_decide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)(w * decide_smem_per_warp<true>())));
+    auto fit = [](auto kernel) {
+        int n = 0;
+        FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0));
+        return std::max(1, n);
+    };
+    fit_.hash[0] = fit(k_hash_count<false>);
+    fit_.hash[1] = fit(k_hash_count<true>);
+    fit_.place = fit(k_place);
+    fit_.scatter = fit(k_scatter);
+    fit_.segsort = fit(k_segsort);
+    fit_.integrate[0] = fit(k_integrate<false>);
+    fit_.integrate[1] = fit(k_integrate<true>);
+    fit_.decide_f64 = fit(k_decide_f64);
+    fit_.integrate_f64 = fit(k_integrate_f64);
+    fit_.compare_f64 = fit(k_compare_f64);
     free_graphs();
 }
 
@@ -592,32 +608,32 @@ GridBuf Engine::grid_buf(int k) const {
 void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool hash, bool fuse_next) {
     device_ahead_ = true;
     const int nfl = (int)table_h_.size();
-    const int sblocks = pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256);
+    // grid of a bird-parallel pass whose kernel fits `f` CTAs per SM
+    auto sgrid = [&](int f) { return pgrid(num_sms_, std::min(shape_.stream_blocks_per_sm, f), V_, 256); };
     const uint32_t ntiles = Btot_ / SCAN_TILE;
     const GridBuf g = grid_buf(buf), gn = grid_buf(buf ^ 1);
     if (ev) FLK_CUDA(cudaEventRecord(ev[0], stream_));
     if (sets)  // a grid-reporting step: the reference's cell hash
-        k_hash_count<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
+        k_hash_count<false><<<sgrid(fit_.hash[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
     else if (hash)
-        k_hash_count<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
+        k_hash_count<true><<<sgrid(fit_.hash[1]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
     if (sets) {
         // a step that reports its grid builds the canonical dense offsets
         // (every bucket, in bucket order) and uses them as the run starts
         k_scan<<<ntiles, SCAN_THREADS, 0, stream_>>>(g.counts, offsets_, ntiles, status_, ctl_);
     } else {
-        k_alloc<<<pgrid(num_sms_, shape_.stream_blocks_per_sm, V_, 256), 256, 0, stream_>>>(table_d_, nfl, g.occ,
-                                                                                           g.counts, offsets_,
-                                                                                           g.occ_count);
+        k_place<<<pgrid(num_sms_, std::min(shape_.stream_blocks_per_sm, fit_.place), Btot_, 1024), 256, 0, stream_>>>(
+            table_d_, nfl, Btot_, g.counts, offsets_, g.occ, g.occ_count);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[2], stream_));
-    k_scatter<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
-    k_segsort<<<pgrid(num_sms_, shape_.segsort_blocks_per_sm, V_, 8), 256, 0, stream_>>>(
+    k_scatter<<<sgrid(fit_.scatter), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, offsets_, tmp_, ctl_);
+    k_segsort<<<pgrid(num_sms_, std::min(shape_.segsort_blocks_per_sm, fit_.segsort), V_, 8), 256, 0, stream_>>>(
         table_d_, nfl, V_, ctl_, g.occ, offsets_, g.counts, g.occ_count, tmp_, ar_, sfwd_, due_, slabs_);
     if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
-        k_decide_f64<<<pgrid(num_sms_, 8, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
+        k_decide_f64<<<pgrid(num_sms_, fit_.decide_f64, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                       g.counts, ar_, dec64_, err64_);
-        k_integrate_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
+        k_integrate_f64<<<sgrid(fit_.integrate_f64), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
@@ -634,10 +650,10 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
                                                                         slabs_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
     if (fuse_next && !sets)
-        k_integrate<true><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
+        k_integrate<true><<<sgrid(fit_.integrate[1]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
     else
-        k_integrate<false><<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
-    if (f64) k_compare_f64<<<sblocks, 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
+        k_integrate<false><<<sgrid(fit_.integrate[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
+    if (f64) k_compare_f64<<<sgrid(fit_.compare_f64), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
 }
 

@@ -198,6 +198,13 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_ = nullptr;  // host<->device state copies of the serving pool
     LaunchShape shape_;
+    // 256-thread CTAs of each grid-stride kernel that fit on one SM at once
+    // (occupancy API, from registers and shared memory); grids never exceed
+    // them, so no CTA waits for a second wave
+    struct Fit {
+        int hash[2] = {8, 8}, place = 8, scatter = 8, segsort = 8, integrate[2] = {8, 8};
+        int decide_f64 = 8, integrate_f64 = 8, compare_f64 = 8;
+    } fit_;
     size_t dev_bytes_ = 0;
 
     // arena (storage order)

@@ -56,11 +56,13 @@ __global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t base, Arena s
 // Counts one CTA iteration of birds into grid buffer g: a thread's bird v
 // (act) falls in bucket b, z-slab `slab`. Bucket counts use one atomic per
 // distinct bucket of a warp and give each bird its arrival rank (slab in the
-// top two bits); the occupied-bucket list gets one atomic per CTA iteration
-// (the first-seen buckets of all eight warps are placed from a shared-memory
-// prefix), so the single list counter is not hit once per warp. Called by all
-// threads of a 256-thread CTA; `it` alternates the shared slots between
-// iterations.
+// top two bits). APPEND (grid-reporting steps): the occupied-bucket list gets
+// one atomic per CTA iteration (the first-seen buckets of all eight warps are
+// placed from a shared-memory prefix), so the single list counter is not hit
+// once per warp; production steps list the occupied buckets in k_place
+// instead. Called by all threads of a 256-thread CTA; `it` alternates the
+// shared slots between iterations.
+template <bool APPEND>
 __device__ __forceinline__ void count_block(bool act, uint32_t v, uint32_t b, uint32_t slab,
                                             uint32_t* __restrict__ arrival, const GridBuf& g,
                                             StepCtl* __restrict__ ctl, uint32_t (&s_first)[2][8], uint32_t it) {
@@ -78,6 +80,7 @@ __device__ __forceinline__ void count_block(bool act, uint32_t v, uint32_t b, ui
         arrival[v] = (rank & 0x3FFFFFFFu) | (slab << 30);
         first = rank == 0;
     }
+    if (!APPEND) return;
     const uint32_t fm = __ballot_sync(FULL, first);
     if (lane == 0) s_first[it][warp] = __popc(fm);
     __syncthreads();
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
                 act = true;
             }
         }
-        count_block(act, v, b, slab, arrival, g, ctl, s_first, it);
+        count_block<!LATTICE>(act, v, b, slab, arrival, g, ctl, s_first, it);
     }
 }
 
@@ -244,47 +247,59 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
 }
 
 // ---------------------------------------------------------------------------
-// pass 2' (steps without grid output): place each occupied bucket's run
+// pass 2' (steps without grid output): list and place the occupied buckets
 // ---------------------------------------------------------------------------
 // Production steps need each occupied bucket's birds contiguous, not the dense
-// canonical offsets, so instead of scanning every bucket this pass gives each
-// occupied bucket a start inside its flock's view region [vbase, vbase + n)
-// from a per-flock cursor: one atomicAdd per warp when the warp's buckets
-// share a flock (the usual case), one per bucket otherwise. Where a run lands
-// does not change any result: decide visits buckets in cell order and each
-// run in bird order. The start is written to offsets[b]; the bucket's length
-// stays in counts[b] until integrate clears it.
-__global__ void __launch_bounds__(256) k_alloc(FlockDesc* __restrict__ fl, int nfl, const uint32_t* __restrict__ occ,
+// canonical offsets. Each warp reads the histogram 128 consecutive buckets at
+// a time (four per lane). A flock's buckets are a power of two, at least
+// 2^16, so every flock's range starts at a multiple of 2^16 and the window
+// lies in one flock. Its occupied buckets get run starts inside the flock's
+// view region [vbase, vbase + n) from the flock's cursor and places in the
+// occupied-bucket list, one atomicAdd on each per window (warp prefix sums in
+// between). The list thus holds lattice rows: consecutive buckets are
+// neighbouring cells along x, so the sort's contiguous bucket ranges, and the
+// deciding birds taken from them in order, are spatial neighbours whose
+// candidates decide's warps share in L1. Where a run lands does not change
+// any result: decide visits buckets in cell order and each run in (slab,
+// bird) order. The start is written to offsets[b]; the bucket's length stays
+// in counts[b] until integrate clears it.
+__global__ void __launch_bounds__(256) k_place(FlockDesc* __restrict__ fl, int nfl, uint32_t nb,
                                                const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
-                                               const uint32_t* __restrict__ occ_count) {
+                                               uint32_t* __restrict__ occ, uint32_t* __restrict__ occ_count) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t nocc = *(volatile const uint32_t*)occ_count;
-    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nocc; i0 += gridDim.x * blockDim.x) {
-        const uint32_t i = i0 + lane;
-        const bool act = i < nocc;
-        uint32_t b = 0, c = 0;
-        int f = -1;
-        if (act) {
-            b = occ[i];
-            c = counts[b];
-            f = find_flock_b(fl, nfl, b);
-        }
-        const uint32_t am = __ballot_sync(FULL, act);
-        const int f0 = __shfl_sync(FULL, f, __ffs(am) - 1);
-        if (__all_sync(FULL, !act || f == f0)) {
-            // one flock: warp prefix of the run lengths + one atomic
-            uint32_t inc = c;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i0 = gw * 128u; i0 < nb; i0 += nw * 128u) {
+        const uint32_t b0 = i0 + 4u * lane;  // nb is a multiple of 2^16: the four lie inside
+        const uint4 c = reinterpret_cast<const uint4*>(counts)[b0 >> 2];
+        const uint32_t n_occ = (c.x != 0) + (c.y != 0) + (c.z != 0) + (c.w != 0);
+        if (!__any_sync(FULL, n_occ != 0)) continue;  // warp-uniform
+        const uint32_t n_birds = c.x + c.y + c.z + c.w;
+        uint32_t ib = n_birds, io = n_occ;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, inc, o);
-                if ((int)lane >= o) inc += y;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t yb = __shfl_up_sync(FULL, ib, o), yo = __shfl_up_sync(FULL, io, o);
+            if ((int)lane >= o) {
+                ib += yb;
+                io += yo;
             }
-            uint32_t base = 0;
-            if (lane == 31) base = atomicAdd(&fl[f0].cursor, inc);
-            base = __shfl_sync(FULL, base, 31) + __ldg(&fl[f0].vbase);
-            if (act) offsets[b] = base + inc - c;
-        } else if (act) {
-            offsets[b] = __ldg(&fl[f].vbase) + atomicAdd(&fl[f].cursor, c);
+        }
+        const int f = find_flock_b(fl, nfl, i0);
+        uint32_t base = 0, obase = 0;
+        if (lane == 31) {
+            base = atomicAdd(&fl[f].cursor, ib);
+            obase = atomicAdd(occ_count, io);
+        }
+        uint32_t run = __shfl_sync(FULL, base, 31) + __ldg(&fl[f].vbase) + ib - n_birds;
+        uint32_t slot = __shfl_sync(FULL, obase, 31) + io - n_occ;
+        const uint32_t cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (cc[k]) {
+                offsets[b0 + k] = run;
+                occ[slot++] = b0 + k;
+                run += cc[k];
+            }
         }
     }
 }

@@ -13,9 +13,9 @@ namespace flk {
 // Works on the buffer the sort pass wrote (parity ^ 1); the last block makes
 // that buffer current. Clears this step's histogram entries (grid buffer cur).
 // FUSE (production runs of several steps): also counts the next step's grid
-// from the new positions into grid buffer nxt (key, arrival rank, histogram,
-// occupied list) for every flock that steps again, so the next step needs no
-// separate hash pass; the counting is count_block, as in k_hash_count.
+// from the new positions into grid buffer nxt (key, arrival rank, histogram)
+// for every flock that steps again, so the next step needs no separate hash
+// pass; the counting is count_block, as in k_hash_count<true>.
 template <bool FUSE>
 __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
                                                    GridBuf cur, GridBuf nxt, uint32_t* __restrict__ key,
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
                 }
             }
         }
-        if (FUSE) count_block(act, v, b, slab, arrival, nxt, ctl, s_first, it);
+        if (FUSE) count_block<false>(act, v, b, slab, arrival, nxt, ctl, s_first, it);
     }
     // the last block to finish advances every active flock and resets the step counters
     __shared__ bool s_last;
