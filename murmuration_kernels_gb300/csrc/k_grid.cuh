@@ -543,7 +543,24 @@ __global__ void __launch_bounds__(256) k_segsort(const FlockDesc* __restrict__ f
         // the run's slab boundaries for decide (runs above 1023 birds are not trimmed)
         if (lane == 0) slabs[b] = L <= 1023u ? (c1 | (c2 << 10) | (c3 << 20)) : 0xFFFFFFFFu;
     }
-    flush_due(sg, lane, due, ctl);
+    // The CTA's remaining records go out in warp order, i.e. in the order of
+    // its consecutive buckets, with one atomic: decide's warps take records in
+    // list order, so each decide CTA works on one compact patch of cells.
+    __shared__ uint32_t s_n[8], s_base;
+    const uint32_t warp = (threadIdx.x >> 5) & 7;
+    if (lane == 0) s_n[warp] = sg.n;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int k = 0; k < 8; ++k) t += s_n[k];
+        s_base = t ? atomicAdd(&ctl->due_count, t) : 0u;
+    }
+    __syncthreads();
+    uint32_t pre = s_base;
+    for (uint32_t k = 0; k < warp; ++k) pre += s_n[k];
+    const uint4* src = reinterpret_cast<const uint4*>(sg.rec);
+    uint4* dst = reinterpret_cast<uint4*>(due + pre);
+    for (uint32_t i = lane; i < sg.n * 3; i += 32) dst[i] = src[i];
 }
 
 }  // namespace flk
