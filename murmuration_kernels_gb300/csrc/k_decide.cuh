@@ -87,6 +87,9 @@ struct Sweep {
 template <bool SETS>
 __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
     const float4 q = __ldg(&w.pos[t + w.shift]);
+    // the neighbour's heading is needed only inside the blind cone, but
+    // loading it here, before the arithmetic, hides the load's latency
+    const float4 fw = __ldg(&w.sfwd[t]);
     const f3 d = mk(__fsub_rn(q.x, w.p.x), __fsub_rn(q.y, w.p.y), __fsub_rn(q.z, w.p.z));
     const float d2 = dot(d, d);
     const float dist = __fsqrt_rn(d2);
@@ -110,7 +113,6 @@ __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
         if (SETS) w.a.h_star += set_mix(j);
     }
     if (dot(w.fi, dh) >= BLIND_COS) {
-        const float4 fw = __ldg(&w.sfwd[t]);
         w.a.align = add(w.a.align, xyz(fw));
         w.a.n_align += 1;
         if (SETS) w.a.h_align += set_mix(j);
