@@ -75,12 +75,13 @@ __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
 // lattice), which costs decide a second cell of candidates each time. Here the
 // cell's coordinates are taken modulo a 2^bx x 2^by x 2^bz lattice (bx + by +
 // bz = log2 buckets, x fastest): cells of a flock narrower than the lattice in
-// every axis (512 m per axis from 2^21 buckets) never share a bucket, and
+// every axis (512 x 512 x 256 m from the 2^20 buckets of 1M birds) never share
+// a bucket, and
 // neighbouring cells along x get neighbouring buckets. Wider flocks wrap, and
 // a cell then shares its bucket with its lattice translate; results do not
 // depend on which cells share buckets.
 __device__ __forceinline__ uint32_t lattice_bucket(int cx, int cy, int cz, uint32_t buckets) {
-    const uint32_t k = 31u - (uint32_t)__clz(buckets);  // buckets = 2^k, k >= 16
+    const uint32_t k = 31u - (uint32_t)__clz(buckets);  // buckets = 2^k, k >= 12: 16+ cells per axis
     const uint32_t bx = (k + 2u) / 3u, by = (k + 1u - bx) >> 1, bz = k - bx - by;
     const uint32_t x = (uint32_t)cx & ((1u << bx) - 1u);
     const uint32_t y = (uint32_t)cy & ((1u << by) - 1u);

@@ -131,7 +131,8 @@ void Engine::free_graphs() {
 size_t Engine::bytes_for(uint32_t n) {
     // state 2 x 68 B (two buffers) + scratch (key, arrival, two occupied lists
     // 4 B each; tmp 8 B; due record 48 B; heading 16 B) + buckets (two
-    // histograms, offsets, slab boundaries 4 B each + status/4096)
+    // histograms, offsets, slab boundaries 4 B each + status/4096; about one
+    // bucket per bird)
     const size_t b = production_buckets(n);
     return (size_t)n * (136 + 88) + b * 16 + (b / SCAN_TILE) * 8 + 256;
 }
@@ -500,13 +501,15 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     table_dirty_ = true;
 }
 
-// Bucket count of a production step: the canonical rule without its 2^22
-// clamp, so flocks above 2M birds keep hash collisions as rare as smaller
-// ones (a production step reports no keys; any count gives the same sets).
+// Bucket count of a production step (one that reports no keys; any count
+// gives the same sets): the power of two at or above n, at least 2^12 (a
+// lattice of at least 16 cells per axis) and at most 2^27. At the flock's
+// density (0.5 birds per m^3, 32 birds per occupied cell) the lattice holds
+// 32 times the flock's volume, so only a flock that spreads far wraps it.
 uint32_t production_buckets(uint32_t n) {
     uint64_t want = 1;
-    while (want < (uint64_t)n * 2) want <<= 1;
-    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 1u << 16), 1u << 27);
+    while (want < (uint64_t)n) want <<= 1;
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 1u << 12), 1u << 27);
 }
 
 void Engine::prepare(bool grid_output) {

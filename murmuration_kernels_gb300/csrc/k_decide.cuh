@@ -514,9 +514,10 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                 // < 3; 10 bits each; all ones: untrimmed). A candidate within the
                 // reach has |dz| <= reach and floor is monotonic, so only slabs
                 // z0..z1 of this cell can hold one: the range shrinks to them.
-                // (A bucket shared by two cells of the box would be swept whole, but
-                // production steps never see one: the box spans at most 3 cells per
-                // axis and the lattice index repeats only every 32 or more.)
+                // (The trim takes the bucket's cell to be this lane's: no two cells of
+                // the box share a bucket in production steps, since the box spans at
+                // most 3 cells per axis and the lattice index repeats only every 16
+                // cells or more.)
                 const uint32_t sw = SETS ? 0xFFFFFFFFu : __ldg(&slabs[b]);  // issued with the range's loads
                 bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
                 if (!SETS && en > s && sw != 0xFFFFFFFFu) {

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
 // Production steps need each occupied bucket's birds contiguous, not the dense
 // canonical offsets. Each warp reads the histogram 128 consecutive buckets at
 // a time (four per lane). A flock's buckets are a power of two, at least
-// 2^16, so every flock's range starts at a multiple of 2^16 and the window
+// 2^12, so every flock's range starts at a multiple of 2^12 and the window
 // lies in one flock. Its occupied buckets get run starts inside the flock's
 // view region [vbase, vbase + n) from the flock's cursor and places in the
 // occupied-bucket list, one atomicAdd on each per window (warp prefix sums in
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_place(FlockDesc* __restrict__ fl, int n
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i0 = gw * 128u; i0 < nb; i0 += nw * 128u) {
-        const uint32_t b0 = i0 + 4u * lane;  // nb is a multiple of 2^16: the four lie inside
+        const uint32_t b0 = i0 + 4u * lane;  // nb is a multiple of 2^12: the four lie inside
         const uint4 c = reinterpret_cast<const uint4*>(counts)[b0 >> 2];
         const uint32_t n_occ = (c.x != 0) + (c.y != 0) + (c.z != 0) + (c.w != 0);
         if (!__any_sync(FULL, n_occ != 0)) continue;  // warp-uniform

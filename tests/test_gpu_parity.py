@@ -297,8 +297,8 @@ def test_grid_reporting_and_production_steps_agree(native, oracle):
 
 
 def test_lattice_wraps_for_flocks_wider_than_the_lattice(native, oracle):
-    # 2^16 production buckets form a 64 x 32 x 32 cell lattice (256 x 128 x 128 m):
-    # a line of small groups 600 m long wraps it several times along x, so
+    # 402 birds get 2^12 production buckets, a 16 x 16 x 16 cell lattice (64 m per
+    # axis): a line of small groups 600 m long wraps it nine times along x, so
     # distant cells share buckets in the production step
     rng = np.random.default_rng(3)
     birds = []
