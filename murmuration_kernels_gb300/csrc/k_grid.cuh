@@ -462,9 +462,9 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned lon
     }
 }
 
-// Five CTAs per SM (48 registers; a few bytes spill in the rarely taken long-
-// run path): the pass waits on its gathers, and 40 warps per SM hide more of
-// that than 32 (the 256-flock batch's sort 0.44 -> 0.42 ms).
+// Five CTAs per SM (48 registers, 36 bytes of spills): the pass waits on its
+// gathers, and 40 warps per SM hide more of that than the 32 that 64
+// registers allow (the 256-flock batch's sort 0.44 -> 0.42 ms).
 __global__ void __launch_bounds__(256, 5) k_segsort(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
