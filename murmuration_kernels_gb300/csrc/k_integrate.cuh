@@ -46,23 +46,29 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
                 const f3 steering = xyz(c);
                 const float roll = a.w;
 
-                const f3 fw = forward(vel);
+                // forward(vel), side_of(forward), |vel| and body_up's cos/sin,
+                // each evaluated once with the helpers' exact operations
+                const float vv = dot(vel, vel);
+                const float vlen = __fsqrt_rn(vv);
+                const f3 fw = vv > 1e-12f ? mul(vel, __fdiv_rn(1.0f, vlen)) : mk(1.f, 0.f, 0.f);
                 const f3 side = side_of(fw);
-                const float speed = fmaxf(len(vel), 1e-6f);
-                const float a_lat = __fdiv_rn(dot(steering, side), MASS);
+                const float speed = fmaxf(vlen, 1e-6f);
+                const float ss = dot(steering, side);
+                const float a_lat = __fdiv_rn(ss, MASS);
                 const float target = clampf(atanf(__fdiv_rn(a_lat, G)), -MAX_BANK, MAX_BANK);
                 const float rate = clampf(__fdiv_rn(__fsub_rn(target, roll), TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
                 const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
 
-                const f3 up = body_up(fw, beta);
-                const float cos_beta = fmaxf(cosf(beta), 0.2f);
+                const float cb = cosf(beta), sb = sinf(beta);
+                const f3 up = add(mul(cross(side, fw), cb), mul(side, sb));  // body_up(fw, beta)
+                const float cos_beta = fmaxf(cb, 0.2f);
                 const float sr = __fdiv_rn(speed, V0);
                 const float sr2 = __fmul_rn(sr, sr);
                 const float lift = __fdiv_rn(__fmul_rn(sr2, L0), cos_beta);
                 const float drag = __fmul_rn(sr2, D0);
                 const f3 flight =
                     sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mul(mul(mk(0.f, 0.f, 1.f), MASS), G));
-                const f3 control = sub(steering, mul(side, dot(steering, side)));
+                const f3 control = sub(steering, mul(side, ss));
                 vel = add(vel, mul(dvs(add(control, flight), MASS), DT));
                 const float sp = len(vel);
                 if (sp > V_MAX) {
