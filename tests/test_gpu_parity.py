@@ -378,6 +378,45 @@ def test_one_million_grid_and_sampled_sets(native, oracle):
     p.close()
 
 
+def test_sixteen_million_grid_and_sampled_sets(native, oracle):
+    """The largest configuration (16,777,216 birds, seed 7): the reference's
+    bucket count is clamped at 2^22 there, so four birds share each bucket and
+    hash collisions are common. Keys, offsets and the stable sorted order are
+    compared whole; neighbour sets, decisions and integrate on a sample (the
+    brute-force oracle tests each sampled bird against all 16.7M)."""
+    n = 16_777_216
+    w = native.generate(n, 7)
+    f = native.Flock(w)
+    dbg = f.step_debug()
+    _, g = f.read()
+    f.close()
+    B = native.buckets_for(n)
+    assert B == 1 << 22
+    keys, offs, srt = oracle.grid(w, B)
+    assert np.array_equal(dbg["keys"], keys)
+    assert np.array_equal(dbg["offsets"], offs)
+    assert np.array_equal(dbg["sorted"], srt)
+    t = np.float32(np.float32(0.0) + np.float32(0.005))
+    want_due = np.nonzero(t >= w[:, 12])[0]
+    rng = np.random.default_rng(11)
+    sample = rng.choice(want_due, size=200, replace=False)
+    sets, dec = oracle.decide_many(w, sample)
+    assert np.array_equal(dbg["sets"][sample], sets)
+    assert np.array_equal(g[sample, 8], dec[:, 3])  # radius
+    assert np.array_equal(g[sample, 13].view(np.uint32), dec[:, 4].view(np.uint32))
+    assert np.abs(g[sample, 9:12] - dec[:, 0:3]).max() <= 1e-5
+    pre = w[sample].copy()
+    pre[:, 9:12] = dec[:, 0:3]
+    post = oracle.integrate_all(pre)
+    assert vec_rel(g[sample, 0:3], post[:, 0:3]).max() <= REL_TOL
+    assert vec_rel(g[sample, 3:6], post[:, 3:6]).max() <= REL_TOL
+    # the production step (lattice buckets, one per bird) decides the same
+    p = native.Flock(w)
+    p.step(1)
+    assert_same_decisions(p.read()[1], g)
+    p.close()
+
+
 # ---- batched and served --------------------------------------------------------
 def test_batched_flocks_equal_plain_runs(native):
     sizes = [1000, 37, 0, 5000, 20_000, 1, 2500, 64_000]
