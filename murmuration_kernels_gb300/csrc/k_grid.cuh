@@ -462,10 +462,11 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned lon
     }
 }
 
-// Five CTAs per SM (48 registers, 36 bytes of spills): the pass waits on its
-// gathers, and 40 warps per SM hide more of that than the 32 that 64
-// registers allow (the 256-flock batch's sort 0.44 -> 0.42 ms).
-__global__ void __launch_bounds__(256, 5) k_segsort(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+// The pass waits on its loads. Each warp loads the bucket descriptors of 32
+// buckets at once (one per lane: bucket, run start, length, flock), and the
+// first 32 keys of the next run while the current one sorts (the 256-flock
+// batch's sort 0.42 -> 0.39 ms, 64 registers, four CTAs per SM).
+__global__ void __launch_bounds__(256, 4) k_segsort(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                  StepCtl* __restrict__ ctl,
                                                  const uint32_t* __restrict__ occ, const uint32_t* __restrict__ offsets,
                                                  const uint32_t* __restrict__ counts,
@@ -483,68 +484,89 @@ __global__ void __launch_bounds__(256, 5) k_segsort(const FlockDesc* __restrict_
     // each warp takes a contiguous range of occupied buckets (neighbouring
     // cells), so a batch of staged records stays spatially close for decide
     const uint32_t per = (nocc + nw - 1) / nw;
-    const uint32_t w_end = min(nocc, gw * per + per);
-    for (uint32_t w = gw * per; w < w_end; ++w) {
-        const uint32_t b = occ[w];
-        const int f = find_flock_b(fl, nfl, b);
-        const FlockDesc d = fl[f];
-        const float t_now = __fadd_rn(d.time, DT);
-        const uint32_t oshift = view_shift(d.sbase, d.vbase, d.parity, ar.cap), nshift = view_shift(d.sbase, d.vbase, d.parity ^ 1u, ar.cap);
-        const uint32_t s0 = __ldg(&offsets[b]), L = __ldg(&counts[b]);
-        // a run lies inside its flock's view region; never otherwise with valid
-        // starts, and skipping keeps every slot inside the flock's own range
-        if (s0 < d.vbase || s0 + L > d.vbase + d.n || s0 + L < s0 || s0 + L > V) {
-            if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
-            continue;
+    const uint32_t w_beg = min(nocc, gw * per), w_end = min(nocc, w_beg + per);
+    for (uint32_t c0 = w_beg; c0 < w_end; c0 += 32) {
+        // the chunk's buckets, starts, lengths and flocks, one per lane, all loads in flight together
+        const uint32_t cnt = min(32u, w_end - c0);
+        uint32_t bl = 0, sl = 0, Ll = 0;
+        int fl_ = 0;
+        if (lane < cnt) {
+            bl = occ[c0 + lane];
+            sl = __ldg(&offsets[bl]);
+            Ll = __ldg(&counts[bl]);
+            fl_ = find_flock_b(fl, nfl, bl);
         }
-        uint32_t c1 = 0, c2 = 0, c3 = 0;
-        if (L <= 32) {
-            unsigned long long x = lane < L ? tmp[s0 + lane] : PAD;
-            x = bitonic32(x, lane);
-            slab_counts(lane < L, x, c1, c2, c3);
-            emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
-        } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
-            unsigned long long x[2];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
-            bitonic_lanes<2>(x, lane);
-#pragma unroll
-            for (int k = 0; k < 2; ++k)
-                slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
-#pragma unroll
-            for (int k = 0; k < 2; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
-                            due, ctl);
-        } else if (L <= 128) {
-            unsigned long long x[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
-            bitonic_lanes<4>(x, lane);
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
-                            due, ctl);
-        } else {
-            // long range (dense cell or hash collision): rank by counting; bird
-            // indices are distinct within a flock, so ranks are distinct
-            for (uint32_t c0 = 0; c0 < L; c0 += 32) {
-                const bool has = c0 + lane < L;
-                const unsigned long long x = has ? tmp[s0 + c0 + lane] : PAD;
-                uint32_t rank = 0;
-                for (uint32_t j0 = 0; j0 < L; j0 += 32) {
-                    const unsigned long long y = (j0 + lane < L) ? tmp[s0 + j0 + lane] : PAD;
-#pragma unroll 8
-                    for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
-                }
-                slab_counts(has, x, c1, c2, c3);
-                emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
+        // the first 32 keys of the next bucket are loaded while this one is sorted
+        auto first_keys = [&](uint32_t j) -> unsigned long long {
+            const uint32_t s = __shfl_sync(FULL, sl, j), l = __shfl_sync(FULL, Ll, j);
+            return (lane < l && s + l >= s && s + l <= V) ? tmp[s + lane] : PAD;
+        };
+        unsigned long long xn = first_keys(0);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint32_t b = __shfl_sync(FULL, bl, j);
+            const int f = __shfl_sync(FULL, fl_, j);
+            const uint32_t s0 = __shfl_sync(FULL, sl, j), L = __shfl_sync(FULL, Ll, j);
+            const unsigned long long x0 = xn;
+            if (j + 1 < cnt) xn = first_keys(j + 1);
+            const FlockDesc d = fl[f];
+            const float t_now = __fadd_rn(d.time, DT);
+            const uint32_t oshift = view_shift(d.sbase, d.vbase, d.parity, ar.cap), nshift = view_shift(d.sbase, d.vbase, d.parity ^ 1u, ar.cap);
+            // a run lies inside its flock's view region; never otherwise with valid
+            // starts, and skipping keeps every slot inside the flock's own range
+            if (s0 < d.vbase || s0 + L > d.vbase + d.n || s0 + L < s0 || s0 + L > V) {
+                if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+                continue;
             }
+            uint32_t c1 = 0, c2 = 0, c3 = 0;
+            if (L <= 32) {
+                unsigned long long x = x0;
+                x = bitonic32(x, lane);
+                slab_counts(lane < L, x, c1, c2, c3);
+                emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
+            } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
+                unsigned long long x[2];
+                x[0] = x0;
+                x[1] = lane + 32u < L ? tmp[s0 + lane + 32u] : PAD;
+                bitonic_lanes<2>(x, lane);
+#pragma unroll
+                for (int k = 0; k < 2; ++k)
+                    slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
+#pragma unroll
+                for (int k = 0; k < 2; ++k)
+                    emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
+                                due, ctl);
+            } else if (L <= 128) {
+                unsigned long long x[4];
+#pragma unroll
+                for (int k = 1; k < 4; ++k) x[k] = lane + 32u * k < L ? tmp[s0 + lane + 32u * k] : PAD;
+                x[0] = x0;
+                bitonic_lanes<4>(x, lane);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    emit_sorted(lane + 32u * k < L, s0 + lane + 32u * k, x[k], d, t_now, lane, ar, oshift, nshift, sfwd, sg,
+                                due, ctl);
+            } else {
+                // long range (dense cell or hash collision): rank by counting; bird
+                // indices are distinct within a flock, so ranks are distinct
+                for (uint32_t k0 = 0; k0 < L; k0 += 32) {
+                    const bool has = k0 + lane < L;
+                    const unsigned long long x = has ? tmp[s0 + k0 + lane] : PAD;
+                    uint32_t rank = 0;
+                    for (uint32_t j0 = 0; j0 < L; j0 += 32) {
+                        const unsigned long long y = (j0 + lane < L) ? tmp[s0 + j0 + lane] : PAD;
+#pragma unroll 8
+                        for (int q = 0; q < 32; ++q) rank += __shfl_sync(FULL, y, q) < x;
+                    }
+                    slab_counts(has, x, c1, c2, c3);
+                    emit_sorted(has, s0 + rank, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
+                }
+            }
+            // the run's slab boundaries for decide (runs above 1023 birds are not trimmed)
+            if (lane == 0) slabs[b] = L <= 1023u ? (c1 | (c2 << 10) | (c3 << 20)) : 0xFFFFFFFFu;
         }
-        // the run's slab boundaries for decide (runs above 1023 birds are not trimmed)
-        if (lane == 0) slabs[b] = L <= 1023u ? (c1 | (c2 << 10) | (c3 << 20)) : 0xFFFFFFFFu;
     }
     // The CTA's remaining records go out in warp order, i.e. in the order of
     // its consecutive buckets, with one atomic: decide's warps take records in
