@@ -89,6 +89,58 @@ __device__ __forceinline__ uint32_t lattice_bucket(int cx, int cy, int cz, uint3
     return x | (y << bx) | (z << (bx + by));
 }
 
+// The cells a deciding bird at p with radius r visits: the box of cells that
+// a search reach of 2r, inflated so that every bird the exact test d2 <= (2r)^2
+// accepts lies in a visited cell (covering the rounding of p -/+ reach as
+// well), touches. `wide` flags an absurd reach (huge or non-finite radius).
+struct SearchBox {
+    float reach, reach2;
+    int lx, ly, lz;
+    long long nx, ny, nz, ncell;
+    bool wide;
+};
+__device__ __forceinline__ SearchBox search_box(f3 p, float r) {
+    SearchBox b;
+    const float rr = __fmul_rn(2.0f, r);
+    const float pm = fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
+    b.reach = rr * 1.00001f + 1e-3f + pm * 1e-6f;
+    b.reach2 = b.reach * b.reach;
+    b.lx = cell1(p.x - b.reach);
+    b.ly = cell1(p.y - b.reach);
+    b.lz = cell1(p.z - b.reach);
+    b.nx = (long long)cell1(p.x + b.reach) - b.lx + 1;
+    b.ny = (long long)cell1(p.y + b.reach) - b.ly + 1;
+    b.nz = (long long)cell1(p.z + b.reach) - b.lz + 1;
+    b.wide = b.nx > (1 << 20) || b.ny > (1 << 20) || b.nz > (1 << 20);
+    b.ncell = b.wide ? (1ll << 62) : b.nx * b.ny * b.nz;
+    return b;
+}
+
+// floor(x / d) = (x * m) >> 16 with m = floor(65536 / d) + 1 holds for x < 32
+// and d <= 32 (m exceeds 65536 / d by at most 1, so the error x / 65536 < 1 / d
+// never reaches the next integer); floor(65536 / d) from an approximate f32
+// quotient is exact here, since 65536 / d is a power of two or at least 1/32
+// away from an integer. m < 2^17.
+__device__ __forceinline__ uint32_t div_magic(uint32_t d) {
+    return __float2uint_rz(__fdividef(65536.0f, (float)d)) + 1u;
+}
+
+// The per-axis bit counts of lattice_bucket for `buckets` (a power of two),
+// packed as bx | by << 5 | bz << 10.
+__device__ __forceinline__ uint32_t lattice_bits(uint32_t buckets) {
+    const uint32_t k = 31u - (uint32_t)__clz(buckets);
+    const uint32_t bx = (k + 2u) / 3u, by = (k + 1u - bx) >> 1, bz = k - bx - by;
+    return bx | (by << 5) | (bz << 10);
+}
+// lattice_bucket with the bit counts given (bits from lattice_bits)
+__device__ __forceinline__ uint32_t lattice_bucket_bits(int cx, int cy, int cz, uint32_t bits) {
+    const uint32_t bx = bits & 31u, by = (bits >> 5) & 31u, bz = (bits >> 10) & 31u;
+    const uint32_t x = (uint32_t)cx & ((1u << bx) - 1u);
+    const uint32_t y = (uint32_t)cy & ((1u << by) - 1u);
+    const uint32_t z = (uint32_t)cz & ((1u << bz) - 1u);
+    return x | (y << bx) | (z << (bx + by));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

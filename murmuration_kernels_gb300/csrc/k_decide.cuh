@@ -359,6 +359,8 @@ __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* _
 template <bool SETS>
 struct WarpSmem {
     static constexpr int NI = SETS ? 8 : 4;  // integer sums per bird
+    int4 box[32];          // the next 32 birds' search boxes (group_boxes)
+    uint4 aux[32];
     uint32_t queue[96];
     float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
     uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
@@ -366,6 +368,36 @@ struct WarpSmem {
     uint32_t vix[32];      // view index (set summaries)
     float pz[32];          // height (roost pull)
 };
+
+// Search boxes of a warp's next 32 deciding birds (records e, e + nw, ...,
+// e + 31 nw), one bird per lane, so the box arithmetic runs once per bird
+// rather than once per lane of a warp-uniform setup. box: first cell x, y;
+// floor(z - reach), floor(z + reach). aux: reach^2 (f32 bits); mx | nx << 17;
+// my | ny << 17 (multiply-shift constants, div_magic); the lattice bit counts
+// (lattice_bits) | 1 << 31 when the box has at most 32 cells (the fast path).
+template <bool SETS>
+__device__ __forceinline__ void group_boxes(WarpSmem<SETS>& m, const DueRec* __restrict__ due, uint32_t e,
+                                            uint32_t nw, uint32_t ndue, uint32_t lane) {
+    const uint32_t ej = e + lane * nw;
+    if (ej < ndue) {
+        const float4 pr = due[ej].pr;
+        const uint32_t buckets = due[ej].fl.z;
+        const SearchBox sb = search_box(mk(pr.x, pr.y, pr.z), pr.w);
+        int4 box = make_int4(sb.lx, sb.ly, 0, 0);
+        uint4 aux = make_uint4(__float_as_uint(sb.reach2), 0u, 0u, 0u);
+        if (sb.ncell <= 32) {
+            const uint32_t nx = (uint32_t)sb.nx, ny = (uint32_t)sb.ny;
+            box.z = (int)floorf(pr.z - sb.reach);
+            box.w = (int)floorf(pr.z + sb.reach);
+            aux.y = div_magic(nx) | (nx << 17);
+            aux.z = div_magic(ny) | (ny << 17);
+            aux.w = lattice_bits(buckets) | (1u << 31);
+        }
+        m.box[lane] = box;
+        m.aux[lane] = aux;
+    }
+    __syncwarp();
+}
 
 // Finishes bird `slot` of the warp's batch (model.rs:95-144), one lane per bird.
 template <bool SETS>
@@ -443,6 +475,9 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
     w.qn = 0;
 
     for (uint32_t e = gw; e < ndue; e += nw) {
+        if (slot == 0) group_boxes<SETS>(m, due, e, nw, ndue, lane);
+        const int4 box = m.box[slot];
+        const uint4 aux = m.aux[slot];
         const DueRec rec = due[e];  // everything the setup needs, one place
         const uint32_t k = __float_as_uint(rec.fk.w);
         const uint32_t st = rec.fl.x, bbase = rec.fl.y, buckets = rec.fl.z;
@@ -455,51 +490,39 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
         w.c2 = __fmul_rn(rr, rr);
         w.self = k;
         const f3 p = w.p;
-        // Search reach: 2r inflated so every bird the exact test d2 <= c2 accepts
-        // lies in a visited cell (covers the rounding of p -/+ reach as well).
-        const float pm = fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
-        const float reach = rr * 1.00001f + 1e-3f + pm * 1e-6f;
-        const float reach2 = reach * reach;
-        const int lx = cell1(p.x - reach), ly = cell1(p.y - reach), lz = cell1(p.z - reach);
-        const long long nxl = (long long)cell1(p.x + reach) - lx + 1, nyl = (long long)cell1(p.y + reach) - ly + 1,
-                        nzl = (long long)cell1(p.z + reach) - lz + 1;
-        // an absurd reach (huge or non-finite radius) takes the brute-force path below
-        const bool wide = nxl > (1 << 20) || nyl > (1 << 20) || nzl > (1 << 20);
-        const long long ncell = wide ? (1ll << 62) : nxl * nyl * nzl;
-        const int nx = (int)nxl, ny = (int)nyl;
 
         w.a.sep = w.a.coh = w.a.align = w.a.csum = mk(0.f, 0.f, 0.f);
         w.a.n_all = w.a.n_star = w.a.n_align = w.a.n_g = 0;
         w.a.h_all = w.a.h_star = w.a.h_align = w.a.h_g = 0;
 
-        if (ncell <= 32) {
-            // fast path: each distinct bucket of the culled box once, no cell check
+        if (aux.w >> 31) {
+            // fast path (search box of at most 32 cells, from group_boxes): each
+            // distinct bucket of the culled box once, no cell check
+            const float reach2 = __uint_as_float(aux.x);
+            const uint32_t nx = aux.y >> 17, ny = aux.z >> 17;
+            const int lx = box.x, ly = box.y, zlo = box.z, zhi = box.w;
+            const int lz = zlo >> 2;  // floor(floor(z - reach) / 4) = floor((z - reach) / 4)
+            const uint32_t ncell = nx * ny * (uint32_t)((zhi >> 2) - lz + 1);
             bool valid = false;
             uint32_t b = 0;
             int z0 = 0, z1 = 3;  // production steps: the z-slabs of this lane's cell within reach
-            if ((long long)lane < ncell) {
-                // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift:
-                // floor(x / d) = (x * m) >> 16 with m = floor(65536 / d) + 1 holds for
-                // x < 32 and d <= 32 (m exceeds 65536 / d by at most 1, so the error
-                // x / 65536 < 1 / d never reaches the next integer); floor(65536 / d)
-                // from an approximate f32 quotient is exact here, since 65536 / d is
-                // a power of two or at least 1/32 away from an integer.
-                const uint32_t mx = __float2uint_rz(__fdividef(65536.0f, (float)nx)) + 1u;
-                const uint32_t my = __float2uint_rz(__fdividef(65536.0f, (float)ny)) + 1u;
-                const uint32_t t = (lane * mx) >> 16;
-                const uint32_t iz = (t * my) >> 16;
-                const int cx = lx + (int)(lane - t * (uint32_t)nx);
-                const int cy = ly + (int)(t - iz * (uint32_t)ny), cz = lz + (int)iz;
+            if (lane < ncell) {
+                // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift (div_magic)
+                const uint32_t t = (lane * (aux.y & 0x1FFFFu)) >> 16;
+                const uint32_t iz = (t * (aux.z & 0x1FFFFu)) >> 16;
+                const int cx = lx + (int)(lane - t * nx);
+                const int cy = ly + (int)(t - iz * ny), cz = lz + (int)iz;
                 if (!SETS) {
-                    z0 = min(3, max(0, (int)floorf(p.z - reach) - 4 * cz));
-                    z1 = min(3, max(0, (int)floorf(p.z + reach) - 4 * cz));
+                    z0 = min(3, max(0, zlo - 4 * cz));
+                    z1 = min(3, max(0, zhi - 4 * cz));
                 }
                 const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
                 const float dx = fminf(fmaxf(p.x, ox), ox + GRID_CELL) - p.x;
                 const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
                 const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
                 valid = dx * dx + dy * dy + dz * dz <= reach2;
-                b = bbase + bucket_of<SETS>(cx, cy, cz, buckets);
+                b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
+                                  : lattice_bucket_bits(cx, cy, cz, aux.w));
             }
             const uint32_t vm = __ballot_sync(FULL, valid);
             bool keep = false;
@@ -537,6 +560,10 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             cand += en - s;
             sweep_packed<SETS>(w, s, en, lane);
         } else {
+            const SearchBox sb = search_box(p, r);
+            const float reach2 = sb.reach2;
+            const int lx = sb.lx, ly = sb.ly, lz = sb.lz;
+            const long long nxl = sb.nx, nyl = sb.ny, ncell = sb.ncell;
             // the flock's own view region [vbase, vbase + n)
             const FlockDesc* fd = &fl[find_flock_v(fl, nfl, k)];
             uint32_t f0 = __ldg(&fd->vbase), f1 = f0 + __ldg(&fd->n);

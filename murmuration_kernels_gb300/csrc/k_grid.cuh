@@ -390,6 +390,7 @@ __device__ __forceinline__ void bitonic_lanes(T (&x)[R], uint32_t lane) {
 // list in batches, one atomic on the list's counter per batch instead of one
 // per bucket (that single counter was hit ~30,000 times per step at 1M birds).
 constexpr uint32_t DUE_STAGE = 64;  // records per warp; flushed once more than 32 wait
+constexpr uint32_t DUE_WORDS = sizeof(DueRec) / 16;  // 16-byte words per record
 
 struct DueStage {
     DueRec* rec;   // this warp's DUE_STAGE records in shared memory
@@ -414,7 +415,7 @@ __device__ __forceinline__ void flush_due(DueStage& sg, uint32_t lane, DueRec* _
     base = __shfl_sync(FULL, base, 0);
     const uint4* src = reinterpret_cast<const uint4*>(sg.rec);
     uint4* dst = reinterpret_cast<uint4*>(due + base);
-    for (uint32_t i = lane; i < sg.n * 3; i += 32) dst[i] = src[i];
+    for (uint32_t i = lane; i < sg.n * DUE_WORDS; i += 32) dst[i] = src[i];
     __syncwarp();
     sg.n = 0;
 }
@@ -585,7 +586,7 @@ __global__ void __launch_bounds__(256, 4) k_segsort(const FlockDesc* __restrict_
     for (uint32_t k = 0; k < warp; ++k) pre += s_n[k];
     const uint4* src = reinterpret_cast<const uint4*>(sg.rec);
     uint4* dst = reinterpret_cast<uint4*>(due + pre);
-    for (uint32_t i = lane; i < sg.n * 3; i += 32) dst[i] = src[i];
+    for (uint32_t i = lane; i < sg.n * DUE_WORDS; i += 32) dst[i] = src[i];
 }
 
 }  // namespace flk
