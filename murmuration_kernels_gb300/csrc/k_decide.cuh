@@ -197,53 +197,6 @@ __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32
     }
 }
 
-// Takes the next non-empty bucket range of the neighbourhood (lane c of s/e),
-// warp-uniform; false when none is left.
-__device__ __forceinline__ bool next_range(uint32_t& km, uint32_t s, uint32_t e, uint32_t& b, uint32_t& end) {
-    if (!km) return false;
-    const int c = __ffs(km) - 1;
-    km &= km - 1;
-    b = __shfl_sync(FULL, s, c);
-    end = __shfl_sync(FULL, e, c);
-    return true;
-}
-
-// Cheap phase over the fast path's bucket ranges, two chunks per iteration.
-template <bool SETS>
-__device__ __forceinline__ void sweep_ranges(Sweep& w, uint32_t km, uint32_t s, uint32_t e, uint32_t lane) {
-    uint32_t b0 = 0, e0 = 0;
-    bool have0 = next_range(km, s, e, b0, e0);
-    while (have0) {
-        uint32_t b1 = 0, e1 = 0;
-        bool have1;
-        if (b0 + 32 < e0) {
-            b1 = b0 + 32;
-            e1 = e0;
-            have1 = true;
-        } else {
-            have1 = next_range(km, s, e, b1, e1);
-        }
-        const uint32_t tA = b0 + lane, tB = b1 + lane;
-        const bool vA = tA < e0 && tA != w.self;
-        const bool vB = have1 && tB < e1 && tB != w.self;
-        float4 qA = make_float4(0.f, 0.f, 0.f, 0.f), qB = qA;
-        if (vA) qA = __ldg(&w.pos[tA + w.shift]);
-        if (vB) qB = __ldg(&w.pos[tB + w.shift]);
-        const bool hA = vA && near<false>(w, qA, 0, 0, 0);
-        const bool hB = vB && near<false>(w, qB, 0, 0, 0);
-        enqueue<SETS>(w, hA, tA, lane);
-        enqueue<SETS>(w, hB, tB, lane);
-        if (!have1) break;
-        if (b1 + 32 < e1) {
-            b0 = b1 + 32;
-            e0 = e1;
-            have0 = true;
-        } else {
-            have0 = next_range(km, s, e, b0, e0);
-        }
-    }
-}
-
 // Cheap phase over the fast path's bucket ranges, packed: the ranges (one
 // per lane, in lane order) are concatenated and swept 32 candidates at a time
 // across range boundaries, two chunks per iteration. The candidates come in
