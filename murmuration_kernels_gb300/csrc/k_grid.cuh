@@ -315,16 +315,37 @@ __global__ void __launch_bounds__(256) k_scatter(const FlockDesc* __restrict__ f
                                                  const uint32_t* __restrict__ key, const uint32_t* __restrict__ arrival,
                                                  const uint32_t* __restrict__ offsets,
                                                  unsigned long long* __restrict__ tmp, StepCtl* __restrict__ ctl) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
-        if (!__ldg(&d->remaining)) continue;
-        const uint32_t bird = ar.id[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
-        const uint32_t arr = arrival[v];
-        const uint32_t pos = __ldg(&offsets[key[v]]) + (arr & 0x3FFFFFFFu);
-        if (pos < V)
-            tmp[pos] = ((unsigned long long)(arr >> 30) << 62) | ((unsigned long long)bird << 31) |
-                       (unsigned long long)(v - __ldg(&d->vbase));
-        else atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+    // two birds per thread and iteration (v and v + stride), so each thread has
+    // two independent load chains in flight
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v0 = blockIdx.x * blockDim.x + threadIdx.x; v0 < V; v0 += 2 * stride) {
+        uint32_t bird[2], arr[2], kk[2], vb[2];
+        bool act[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const uint32_t v = v0 + u * stride;
+            act[u] = false;
+            if (v < V) {
+                const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
+                if (__ldg(&d->remaining)) {
+                    act[u] = true;
+                    vb[u] = __ldg(&d->vbase);
+                    bird[u] = ar.id[v + view_shift(__ldg(&d->sbase), vb[u], __ldg(&d->parity), ar.cap)];
+                    arr[u] = arrival[v];
+                    kk[u] = key[v];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!act[u]) continue;
+            const uint32_t v = v0 + u * stride;
+            const uint32_t pos = __ldg(&offsets[kk[u]]) + (arr[u] & 0x3FFFFFFFu);
+            if (pos < V)
+                tmp[pos] = ((unsigned long long)(arr[u] >> 30) << 62) | ((unsigned long long)bird[u] << 31) |
+                           (unsigned long long)(v - vb[u]);
+            else atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+        }
     }
 }
 
