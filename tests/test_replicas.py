@@ -71,3 +71,24 @@ def test_single_process_needs_no_process_group():
         for k, v in saved.items():
             if v is not None:
                 os.environ[k] = v
+
+
+def test_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference (the oracle port timed on the host cores) runs
+    without a GPU and prints one JSON line with the reference-arm fields."""
+    import json
+    import subprocess
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--birds", "20000",
+                        "--steps", "2", "--warmup", "1", "--cpu-budget", "0.5"],
+                       capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "bird-updates/s" and d["value"] > 0
+    assert d["steps"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1 and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["birds"] == 20000
