@@ -291,6 +291,21 @@ def pass_bandwidths(r, n):
             "integrate": gbs(80, p["integrate_ms"])}
 
 
+def bench_multi_step(m, args, local):
+    """The same workload as the library runs it for flk_step(K): 10-step CUDA
+    graphs, each step's integrate also counting the next step's grid, no L2
+    flush between steps (device time, CUDA events). Not the headline: the
+    headline flushes L2 before every single-step launch."""
+    n, K = args.birds, args.steps
+    b = m.Batch(device=local)
+    b.add(m.generate(n, args.seed))
+    b.step(max(10, args.warmup))  # warm-up and graph capture
+    ms = b.time_steps(K)
+    b.close()
+    return {"value": n * K / (ms / 1e3), "unit": "bird-updates/s", "ms_per_step": ms / K,
+            "how": f"{K} steps in 10-step CUDA graphs (fused integrate and next hash), no L2 flush between steps"}
+
+
 def bench_e2e(m, args, local):
     """Through the C ABI with host buffers: upload, K steps, download."""
     n, K = args.birds, args.steps
@@ -466,6 +481,7 @@ def main():
     }
     if rank == 0:
         out["e2e"] = bench_e2e(m, args, local)
+        out["multi_step"] = bench_multi_step(m, args, local)
         if not args.no_extra:
             out["batched"] = bench_batched(m, args, local)
             out["served"] = bench_served(m, args, local)
