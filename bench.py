@@ -472,6 +472,12 @@ def main():
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,
                      "traffic": traffic},
+        # what bounds the step: decide's share of the eager pass times (live) and its
+        # limiter, from the committed ncu summary of the same workload
+        "dominant_kernel": {"name": "k_decide", "share_of_step": r["passes"]["decide_ms"] / r["passes"]["total_ms"]
+                            if r["passes"]["total_ms"] > 0 else None,
+                            "bound": "instruction issue (not HBM: ~65 MB of DRAM traffic per launch)",
+                            "evidence": "profiles/decide_1m_current.txt"},
         "passes_ms": {k: round(v, 5) for k, v in r["passes"].items() if k.endswith("_ms")},
         "decide": decide_rates(r, n),
         "passes_gbs": pass_bandwidths(r, n),
