@@ -12,15 +12,19 @@
 // Each bucket's birds are contiguous in the flock's state, which the sort
 // pass has just written in cell order (view index t lives in slot t + shift of
 // the reordered buffer), so the lanes of a warp read coalesced runs of
-// positions. The sweep is split in two: the cheap phase computes d2 for every
-// candidate and appends the indices of those within 2R to a per-warp queue in
-// shared memory (ballot + popc); whenever 32 hits are queued, the whole warp
-// processes them together in the expensive phase (sqrt, three IEEE divisions,
-// the separation Gaussian, blind-angle test). Only ~14 % of candidates are
-// hits, so this keeps the expensive code on full warps instead of running it
-// for one or two lanes. The cheap phase sweeps the bucket ranges as one packed
-// sequence, two 32-candidate chunks per iteration (two loads in flight per
-// lane, tested together with paired f32x2 arithmetic).
+// positions. In production steps each run is ordered by 1 m z-slab and the
+// sort recorded the slab boundaries, so every visited cell's run is narrowed
+// to the slabs the bird's z-reach touches. The sweep is split in two: the
+// cheap phase computes d2 for every candidate and appends the indices of those
+// within 2R to a per-warp queue in shared memory (ballot + popc); whenever 32
+// hits are queued, the whole warp processes them together in the expensive
+// phase (sqrt, three IEEE divisions, the separation Gaussian, blind-angle
+// test). Only ~19 % of candidates are hits, so this keeps the expensive code on
+// full warps instead of running it for a few lanes. The cheap phase sweeps the
+// bucket ranges as one packed sequence, two 32-candidate chunks per iteration
+// (two loads in flight per lane, tested together with paired f32x2 arithmetic).
+// The per-bird box arithmetic runs one bird per lane for a warp's next 32
+// birds (group_boxes), not warp-uniformly.
 //
 // Per-lane partial sums are reduced with a transposed (reduce-scatter)
 // shuffle pattern straight into shared memory; once 32 birds are reduced, all
