@@ -121,6 +121,9 @@ int flk_batch_step_debug(flk_batch* b, const int32_t* ids, uint32_t count, uint3
  * gives it. A duplicated id is FLK_ERR_ARG. */
 int flk_batch_step_f64(flk_batch* b, const int32_t* ids, uint32_t count, double* out64, double* reports);
 int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t decide_threads, int32_t graph_chunk);
+/* Chunk graphs instantiated, and updated in place (cudaGraphExecUpdate, when
+ * only sizes or pointers changed, e.g. a flock joined or left), so far. */
+int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated);
 int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
 /* Times `steps` graph-launched steps on the batch's stream with CUDA events. */
 int flk_batch_time_steps(flk_batch* b, uint32_t steps, double* ms);

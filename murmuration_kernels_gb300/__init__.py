@@ -86,6 +86,7 @@ _SIGS = {
     "flk_batch_read": (C.c_int, [_P, C.c_int32, _PF, _PF]),
     "flk_batch_step_debug": (C.c_int, [_P, _PI, C.c_uint32, _PU, _PU, _PU, _PU]),
     "flk_batch_step_f64": (C.c_int, [_P, _PI, C.c_uint32, _PD, _PD]),
+    "flk_batch_graph_counts": (C.c_int, [_P, _PU64, _PU64]),
     "flk_batch_tune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "flk_batch_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
     "flk_batch_time_steps": (C.c_int, [_P, C.c_uint32, _PD]),
@@ -389,6 +390,12 @@ class Batch:
             res.append((out[k:k + n], _f64_report(rep[i])))
             k += n
         return res
+
+    def graph_counts(self) -> tuple[int, int]:
+        """(chunk graphs instantiated, chunk graphs updated in place) so far."""
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib().flk_batch_graph_counts(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def tune(self, stream_bps: int = 0, decide_bps: int = 0, decide_threads: int = 0, graph_chunk: int = 0) -> None:
         _check(lib().flk_batch_tune(self._h, stream_bps, decide_bps, decide_threads, graph_chunk))

@@ -381,6 +381,12 @@ extern "C" int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_b
     });
 }
 
+extern "C" int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated) {
+    if (!b || !instantiated || !updated) return fail(FLK_ERR_ARG, "flk_batch_graph_counts: null pointer");
+    b->eng->graph_counts(instantiated, updated);
+    return FLK_OK;
+}
+
 extern "C" int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* cand, uint64_t* pairs) {
     if (!b) return fail(FLK_ERR_ARG, "flk_batch_counters: null handle");
     return guarded([&] {

@@ -110,7 +110,7 @@ Engine::~Engine() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
     if (copy_) cudaStreamSynchronize(copy_);
-    free_graphs();
+    destroy_graphs();
     dfree(ar_.A); dfree(ar_.B); dfree(ar_.C); dfree(ar_.D); dfree(ar_.id);
     dfree(table_d_);
     dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(occ2_); dfree(due_);
@@ -122,10 +122,16 @@ Engine::~Engine() {
     if (stream_) cudaStreamDestroy(stream_);
 }
 
-void Engine::free_graphs() {
+// Marks the captured chunk as out of date (sizes, pointers or launch shapes
+// changed); the next ensure_graph recaptures it and updates the executable
+// graph in place.
+void Engine::free_graphs() { graph_stale_ = true; }
+
+void Engine::destroy_graphs() {
     if (graph_) cudaGraphExecDestroy(graph_);
     graph_ = nullptr;
     graph_steps_ = 0;
+    graph_stale_ = false;
 }
 
 size_t Engine::bytes_for(uint32_t n) {
@@ -664,18 +670,35 @@ void Engine::enqueue_steps(uint32_t n) {
     for (uint32_t i = 0; i < n; ++i) enqueue_step(false, nullptr, false, (int)(i & 1u), i == 0, i + 1 < n);
 }
 
+// A chunk of `graph_chunk` steps as one CUDA graph. When only sizes, pointers
+// or launch shapes changed since the last capture (a flock joined or left, a
+// buffer grew), the new capture has the same nodes, and cudaGraphExecUpdate
+// rewrites the executable graph's parameters instead of instantiating a new
+// one (launches already in flight keep their old parameters). A different
+// chunk length, or an update the runtime refuses, instantiates afresh.
 void Engine::ensure_graph() {
     const uint32_t chunk = (uint32_t)std::max(1, shape_.graph_chunk);
-    if (graph_ && graph_steps_ == chunk) return;
-    free_graphs();
+    if (graph_ && graph_steps_ == chunk && !graph_stale_) return;
     cudaGraph_t g;
     FLK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     enqueue_steps(chunk);
     FLK_CUDA(cudaStreamEndCapture(stream_, &g));
+    if (graph_ && graph_steps_ == chunk) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(graph_, g, &info) == cudaSuccess) {
+            cudaGraphDestroy(g);
+            graph_stale_ = false;
+            ++graph_updates_;
+            return;
+        }
+        (void)cudaGetLastError();  // the refused update leaves no sticky error
+    }
+    destroy_graphs();
     cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
     cudaGraphDestroy(g);
     FLK_CUDA(e);
     graph_steps_ = chunk;
+    ++graph_instantiations_;
 }
 
 void Engine::run(uint32_t steps) {

@@ -165,6 +165,11 @@ public:
     size_t device_bytes() const { return dev_bytes_; }
     // Cumulative counters from the step-control block.
     void counters(unsigned long long* due, unsigned long long* cand, unsigned long long* pairs);
+    // Chunk graphs instantiated, and updated in place, so far.
+    void graph_counts(uint64_t* instantiated, uint64_t* updated) const {
+        *instantiated = graph_instantiations_;
+        *updated = graph_updates_;
+    }
     // Bytes of device memory a flock of n birds would add (state + scratch).
     static size_t bytes_for(uint32_t n);
     // Launches of engine kernels per step (for the bench's launch count).
@@ -191,6 +196,7 @@ private:
     void enqueue_steps(uint32_t n);
     GridBuf grid_buf(int k) const;
     void free_graphs();
+    void destroy_graphs();
     void ensure_graph();
     void sync_times();
 
@@ -248,6 +254,8 @@ private:
 
     cudaGraphExec_t graph_ = nullptr;
     uint32_t graph_steps_ = 0;
+    bool graph_stale_ = false;  // parameters changed since the capture (free_graphs)
+    uint64_t graph_instantiations_ = 0, graph_updates_ = 0;
 };
 
 // Canonical bucket count for a flock of n birds (reference cuda/flock.cu:368-372).

@@ -677,3 +677,27 @@ def test_pool_error_report_evaluates_a_live_flock_without_advancing_it(native):
     tp, wp = p.read()
     p.close()
     assert tp == t1 and wp.tobytes() == w1.tobytes()
+
+
+def test_chunk_graph_is_updated_in_place_when_flocks_join_and_leave(native):
+    """A flock joining or leaving changes only the chunk graph's sizes and
+    pointers: the executable graph is updated (cudaGraphExecUpdate), not
+    instantiated again, and every flock still ends exactly as when run alone."""
+    ws = [native.generate(n, s) for n, s in [(3000, 1), (5000, 2), (2000, 3)]]
+    b = native.Batch()
+    ids = [b.add(w) for w in ws[:2]]
+    b.step(10)
+    assert b.graph_counts() == (1, 0)
+    ids.append(b.add(ws[2]))
+    b.step(10)
+    b.remove(ids[0])
+    b.step(10)
+    assert b.graph_counts() == (1, 2)
+    for fid, w, k in [(ids[1], ws[1], 30), (ids[2], ws[2], 20)]:
+        f = native.Flock(w)
+        f.step(k)
+        t, g = f.read()
+        f.close()
+        tb, gb = b.read(fid)
+        assert t == tb and g.tobytes() == gb.tobytes()
+    b.close()
