@@ -291,6 +291,30 @@ def pass_bandwidths(r, n):
             "integrate": gbs(80, p["integrate_ms"])}
 
 
+# decide's warp instructions per launch at 1M birds (seed 1), from the committed
+# ncu summary (smsp__inst_executed.sum); 4 warp instructions per clock per SM peak
+DECIDE_INST_1M = 120.5e6
+GB300_SMS = 152
+
+
+def dominant_kernel(r, n, seed):
+    """decide's share of the step (live) and its limiter: instruction issue. For
+    the 1M-bird, seed-1 step, the achieved issue rate is the profiled
+    instruction count over the live decide time, against 4 warp instructions
+    per clock per SM at the sampled SM clock."""
+    p = r["passes"]
+    out = {"name": "k_decide", "share_of_step": p["decide_ms"] / p["total_ms"] if p["total_ms"] > 0 else None,
+           "bound": "instruction issue (not HBM: ~65 MB of DRAM traffic per launch)",
+           "evidence": "profiles/decide_1m_current.txt"}
+    mhz = (r["clocks"] or {}).get("sm_mhz")
+    if (n, seed) == (1_000_000, 1) and p["decide_ms"] > 0 and mhz:
+        achieved = DECIDE_INST_1M / (p["decide_ms"] / 1e3)
+        peak = 4.0 * GB300_SMS * mhz * 1e6
+        out.update({"issue_achieved": achieved, "issue_peak": peak, "issue_unit": "warp instructions/s",
+                    "issue_frac": achieved / peak})
+    return out
+
+
 def bench_multi_step(m, args, local):
     """The same workload as the library runs it for flk_step(K): 10-step CUDA
     graphs, each step's integrate also counting the next step's grid, no L2
@@ -483,10 +507,7 @@ def main():
                      "traffic": traffic},
         # what bounds the step: decide's share of the eager pass times (live) and its
         # limiter, from the committed ncu summary of the same workload
-        "dominant_kernel": {"name": "k_decide", "share_of_step": r["passes"]["decide_ms"] / r["passes"]["total_ms"]
-                            if r["passes"]["total_ms"] > 0 else None,
-                            "bound": "instruction issue (not HBM: ~65 MB of DRAM traffic per launch)",
-                            "evidence": "profiles/decide_1m_current.txt"},
+        "dominant_kernel": dominant_kernel(r, n, args.seed),
         "passes_ms": {k: round(v, 5) for k, v in r["passes"].items() if k.endswith("_ms")},
         "decide": decide_rates(r, n),
         "passes_gbs": pass_bandwidths(r, n),
