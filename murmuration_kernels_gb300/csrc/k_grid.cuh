@@ -542,14 +542,24 @@ __global__ void __launch_bounds__(256, 4) k_segsort(const FlockDesc* __restrict_
             uint32_t c1 = 0, c2 = 0, c3 = 0;
             if (L <= 32) {
                 unsigned long long x = x0;
-                x = bitonic32(x, lane);
+                // runs often arrive in order already (birds are counted in the previous
+                // step's cell order, a warp's birds with consecutive ranks)
+                const unsigned long long nx = __shfl_down_sync(FULL, x, 1);
+                if (!__all_sync(FULL, lane + 1 >= L || x < nx)) x = bitonic32(x, lane);
                 slab_counts(lane < L, x, c1, c2, c3);
                 emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
             } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
                 unsigned long long x[2];
                 x[0] = x0;
                 x[1] = lane + 32u < L ? tmp[s0 + lane + 32u] : PAD;
-                bitonic_lanes<2>(x, lane);
+                {
+                    const unsigned long long n0 = __shfl_down_sync(FULL, x[0], 1);
+                    const unsigned long long h1 = __shfl_sync(FULL, x[1], 0);
+                    const unsigned long long n1 = __shfl_down_sync(FULL, x[1], 1);
+                    const bool ok0 = lane < 31 ? x[0] < n0 : x[0] < h1;
+                    const bool ok1 = lane + 33u >= L || x[1] < n1;
+                    if (!__all_sync(FULL, ok0 && ok1)) bitonic_lanes<2>(x, lane);
+                }
 #pragma unroll
                 for (int k = 0; k < 2; ++k)
                     slab_counts(lane + 32u * k < L, x[k], c1, c2, c3);
