@@ -545,7 +545,23 @@ __global__ void __launch_bounds__(256, 4) k_segsort(const FlockDesc* __restrict_
                 // runs often arrive in order already (birds are counted in the previous
                 // step's cell order, a warp's birds with consecutive ranks)
                 const unsigned long long nx = __shfl_down_sync(FULL, x, 1);
-                if (!__all_sync(FULL, lane + 1 >= L || x < nx)) x = bitonic32(x, lane);
+                const uint32_t dm = __ballot_sync(FULL, lane + 1 < L && x > nx);  // descents
+                if (dm && (dm & (dm - 1))) {
+                    x = bitonic32(x, lane);
+                } else if (dm) {
+                    // two ascending runs, lanes [0, k) and [k, L): with the second reversed
+                    // into the top lanes and padding between, the 32 keys form a bitonic
+                    // sequence, which one merge cascade sorts
+                    const uint32_t k = (uint32_t)__ffs(dm), lb = L - k;
+                    const uint32_t src = k + 31u - lane;  // lanes >= 32 - lb take B reversed
+                    const unsigned long long y = __shfl_sync(FULL, x, src & 31u);
+                    x = lane < k ? x : (lane >= 32u - lb ? y : PAD);
+#pragma unroll
+                    for (int j = 16; j > 0; j >>= 1) {
+                        const unsigned long long z = __shfl_xor_sync(FULL, x, j);
+                        x = (lane & (uint32_t)j) ? kmax(x, z) : kmin(x, z);
+                    }
+                }
                 slab_counts(lane < L, x, c1, c2, c3);
                 emit_sorted(lane < L, s0 + lane, x, d, t_now, lane, ar, oshift, nshift, sfwd, sg, due, ctl);
             } else if (L <= 64) {  // two cells in one bucket, or a dense cell: sort in registers
