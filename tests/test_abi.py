@@ -110,3 +110,20 @@ def test_file_info_reads_the_header(native, tmp_path):
     with pytest.raises(native.FlockError) as e:
         native.file_info(str(bad))
     assert e.value.code == -7
+
+
+def test_header_is_plain_c(native, tmp_path):
+    """include/flock_gb300.h is the FFI boundary: it compiles as strict C99 (what
+    bindgen, cgo or a C caller sees) and as C++."""
+    import os
+    import shutil
+
+    hdr_dir = os.path.dirname(native.HEADER)
+    src = tmp_path / "use.c"
+    src.write_text('#include "flock_gb300.h"\nint main(void) { return flk_buckets_for(10) == 0; }\n')
+    for cc, extra in (("gcc", ["-std=c99", "-pedantic", "-Werror"]), ("g++", ["-x", "c++", "-std=c++11", "-Werror"])):
+        if shutil.which(cc) is None:
+            pytest.skip(f"{cc} not available")
+        r = subprocess.run([cc, *extra, "-Wall", "-Wextra", "-I" + hdr_dir, "-c", str(src), "-o",
+                            str(tmp_path / "use.o")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
