@@ -22,7 +22,7 @@
 // test). Only ~19 % of candidates are hits, so this keeps the expensive code on
 // full warps instead of running it for a few lanes. The cheap phase sweeps the
 // bucket ranges as one packed sequence, two 32-candidate chunks per iteration
-// (two loads in flight per lane, tested together with paired f32x2 arithmetic).
+// (two loads in flight per lane).
 // The per-bird box arithmetic runs one bird per lane for a warp's next 32
 // birds (group_boxes), not warp-uniformly.
 //
@@ -177,16 +177,15 @@ __device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int
     return hit;
 }
 
-// near<false> for two candidates at once with paired f32 arithmetic (each
-// element rounded to nearest, so bit-identical to two scalar tests).
+// near<false> for two candidates. Set membership must round exactly as the
+// oracle's chain of separately rounded f32 operations, so the test stays in
+// scalar round-to-nearest intrinsics: paired f32x2 multiplies and adds (the
+// __fmul2_rn/__fadd2_rn intrinsics, or mul.rn/add.rn.f32x2 in PTX) were
+// measured to round d2 differently, admitting a bird one ulp outside 2R
+// (test_two_birds_one_ulp_outside_2r), and cost no time to give up.
 __device__ __forceinline__ void near2(const Sweep& w, const float4 qa, const float4 qb, bool& ha, bool& hb) {
-    const float2 np = make_float2(-w.p.x, -w.p.x), nq = make_float2(-w.p.y, -w.p.y), nr = make_float2(-w.p.z, -w.p.z);
-    const float2 dx = __fadd2_rn(make_float2(qa.x, qb.x), np);
-    const float2 dy = __fadd2_rn(make_float2(qa.y, qb.y), nq);
-    const float2 dz = __fadd2_rn(make_float2(qa.z, qb.z), nr);
-    const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-    ha = d2.x <= w.c2;
-    hb = d2.y <= w.c2;
+    ha = near<false>(w, qa, 0, 0, 0);
+    hb = near<false>(w, qb, 0, 0, 0);
 }
 
 // Cheap phase over one contiguous candidate range [sc, ec) (wide paths).
@@ -263,7 +262,7 @@ __device__ __forceinline__ void drain(Sweep& w, uint32_t lane) {
 
 // Reduce-scatter of K = 2^m values across the warp: afterwards lane l holds the
 // warp total of value index (l >> (5 - m)) & (K - 1) (fixed association). The
-// float version adds value pairs with f32x2 (each element rounded to nearest).
+// float version adds value pairs with f32x2 additions (sums, not set membership).
 template <int K>
 __device__ __forceinline__ float rs_float(float (&v)[K], uint32_t lane) {
 #pragma unroll

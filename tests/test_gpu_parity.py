@@ -227,6 +227,23 @@ def colliding_cells(mask: int, count: int = 2, near: bool = False):
     raise AssertionError("no colliding pair found")
 
 
+def test_two_birds_one_ulp_outside_2r(native, oracle):
+    """A pair met in a settled 1M-bird flock: the neighbour's d2, rounded as the
+    oracle's chain of f32 operations, lies one ulp above (2r)^2 (the exactly
+    rounded d2 would equal it). It must stay outside the 2R (centrality) set in
+    both kinds of step."""
+    import struct
+
+    def f(h):
+        return np.frombuffer(struct.pack("<I", h), dtype=np.float32)[0]
+
+    w = np.stack([bird((f(0xC258C08B), f(0x41168935), f(0x431F1A43)), radius=f(0x3FC7564B), next_decision=0.0),
+                  bird((f(0xC24C9446), f(0x410D4422), f(0x431F6CD9)), next_decision=1.0)])
+    sets, dec = oracle.decide_many(w, np.array([0]))
+    assert sets[0, 3] == 0  # the oracle: nobody within 2R
+    assert_step_parity(native, oracle, w)
+
+
 def test_hash_collisions(native, oracle):
     mask = native.buckets_for(40) - 1
     rng = np.random.default_rng(1)
@@ -284,6 +301,9 @@ def assert_same_decisions(ga, gb):
     if len(ga):
         assert vec_rel(ga[:, 0:3], gb[:, 0:3]).max() <= REL_TOL
         assert vec_rel(ga[:, 3:6], gb[:, 3:6]).max() <= REL_TOL
+        # centrality (|sum over the 2R set| / its size): a 2R set that differs
+        # by one bird moves it far beyond rounding
+        assert np.abs(ga[:, 14].astype(np.float64) - gb[:, 14]).max() <= 1e-5
 
 
 def test_grid_reporting_and_production_steps_agree(native, oracle):
