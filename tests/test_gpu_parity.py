@@ -462,6 +462,30 @@ def test_sixteen_million_grid_and_sampled_sets(native, oracle):
     p.close()
 
 
+def test_settled_million_every_bird_against_the_cpu_grid(native, oracle):
+    """1M birds (seed 1) after 130 GPU steps, a flocking state: one more step,
+    production and grid-reporting, against the oracle's grid restatement from the
+    same state, every bird. The grid restatement decides exactly as the
+    brute-force oracle (same membership tests, test_oracle), so neighbour counts,
+    radii and next decisions must be equal, and centrality, whose 2R set a single
+    extra or missing bird moves by ~1/n, must agree to rounding."""
+    f = native.Flock(native.generate(1_000_000, 1))
+    f.step(130)
+    t0, w = f.read()
+    f.close()
+    t_cpu, c = oracle.step_grid(w, t0)
+    for debug in (False, True):
+        g = native.Flock(w, t0)
+        if debug:
+            g.step_debug()
+        else:
+            g.step(1)
+        t_gpu, s = g.read()
+        g.close()
+        assert t_gpu == np.float32(t_cpu)
+        assert_state_parity(s, c, oracle)
+
+
 # ---- batched and served --------------------------------------------------------
 def test_batched_flocks_equal_plain_runs(native):
     sizes = [1000, 37, 0, 5000, 20_000, 1, 2500, 64_000]
