@@ -486,6 +486,27 @@ def test_settled_million_every_bird_against_the_cpu_grid(native, oracle):
         assert_state_parity(s, c, oracle)
 
 
+def test_settled_sixteen_million_every_bird_against_the_cpu_grid(native, oracle):
+    """The largest configuration (16,777,216 birds, seed 7) 40 steps in: one more
+    step of each kind against the oracle's grid restatement, every bird (the
+    grid-reporting step with the reference's bucket count clamped at 2^22)."""
+    f = native.Flock(native.generate(16_777_216, 7))
+    f.step(40)
+    t0, w = f.read()
+    f.close()
+    t_cpu, c = oracle.step_grid(w, t0)
+    for debug in (False, True):
+        g = native.Flock(w, t0)
+        if debug:
+            g.step_debug()
+        else:
+            g.step(1)
+        t_gpu, s = g.read()
+        g.close()
+        assert t_gpu == np.float32(t_cpu)
+        assert_state_parity(s, c, oracle)
+
+
 # ---- batched and served --------------------------------------------------------
 def test_batched_flocks_equal_plain_runs(native):
     sizes = [1000, 37, 0, 5000, 20_000, 1, 2500, 64_000]
