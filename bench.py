@@ -261,8 +261,10 @@ def bench_plain(m, args, dist, local):
     # per-pass shares from an eager run with events between passes (same state continues)
     passes = f.step_timed(10, 0)
     due1, cand1, pairs1 = f.counters()
+    # the next step's f32 error against the same step evaluated in FP64 (flk_step_f64)
+    _, fp64 = f.step_f64()
     f.close()
-    return dict(ms=ms, total_ms=total_ms, clocks=clk.summary(), passes=passes,
+    return dict(ms=ms, total_ms=total_ms, clocks=clk.summary(), passes=passes, fp64=fp64,
                 due_frac=(due1 - due0) / (10 * n), cand_per_due=(cand1 - cand0) / max(1, due1 - due0),
                 pairs_per_due=(pairs1 - pairs0) / max(1, due1 - due0), due_total=due0)
 
@@ -293,7 +295,7 @@ def pass_bandwidths(r, n):
 
 # decide's warp instructions per launch at 1M birds (seed 1), from the committed
 # ncu summary (smsp__inst_executed.sum); 4 warp instructions per clock per SM peak
-DECIDE_INST_1M = 120.5e6
+DECIDE_INST_1M = 122.1e6
 GB300_SMS = 152
 
 
@@ -512,6 +514,9 @@ def main():
         "decide": decide_rates(r, n),
         "passes_gbs": pass_bandwidths(r, n),
         "gpu_launches": m.kernels_per_step() * K,
+        "fp64_error": dict(r["fp64"], how="one more f32 step against the same step in FP64 from the same state "
+                                          "(max relative position / velocity error over all birds; neighbour-count "
+                                          "mismatches)"),
         "clocks": r["clocks"],
         "step_ms_p50": float(np.median(r["ms"])), "step_ms_min": float(r["ms"].min()),
     }
