@@ -80,8 +80,9 @@ def tune(batch, steps: int = 10, reps: int = 2, margin: float = 0.01, gpu: str =
     best_t = _time(batch, best, steps, reps)
     trials = 1
     for knob, values in SPACE.items():
+        start = best[knob]  # timed already, as part of the incumbent
         for v in values:
-            if v == best[knob]:
+            if v == start or v == best[knob]:
                 continue
             cand = dict(best, **{knob: v})
             t = _time(batch, cand, steps, reps)
