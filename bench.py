@@ -96,6 +96,10 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "10"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a moment to start: the region begins once it samples
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self

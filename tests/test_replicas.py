@@ -92,3 +92,22 @@ def test_reference_arm_prints_the_contract_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["birds"] == 20000
+
+
+def test_clock_summary_parses_nvidia_smi_rows(tmp_path):
+    """bench.py's clock record: median SM clock under load, the maximum, and every
+    throttle reason seen active during the region."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    rows = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+            "0, 1995, 2070, 1200.5, 0x4, Not Active, Not Active, Not Active, Active",
+            "0, 2040, 2070, 1100.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+            "garbage line"]
+    path = tmp_path / "clocks.csv"
+    path.write_text("\n".join(rows) + "\n")
+    c = bench.ClockSampler(0)
+    c.proc, c.path = object(), str(path)
+    s = c.summary()
+    assert s == {"sm_mhz": 2040.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert not path.exists()
