@@ -78,7 +78,8 @@ int flk_size(const flk_flock* f, uint32_t* n, uint32_t* buckets);
  *                    birds that did not decide.
  * Any output pointer may be NULL. */
 int flk_step_debug(flk_flock* f, uint32_t* keys, uint32_t* offsets, uint32_t* sorted, uint32_t* sets);
-/* Cumulative deciding birds, candidate tests and pairs within 2R. */
+/* Cumulative deciding birds, candidate tests and pairs within 2R (counters of
+ * the decide pass, cuda/flock.cu:190-290; the reference keeps none). */
 int flk_counters(flk_flock* f, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
 /* One step (exactly flk_step(f, 1)) that also evaluates the same step in FP64
  * from the same input state, for error reports on a live flock. `out64`
@@ -94,45 +95,59 @@ int flk_step_f64(flk_flock* f, double* out64, double* report);
  * the step starts with a cold L2, then brackets the step with CUDA events on
  * the library's stream. ms_per_step[steps] receives each step's device time. */
 int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step);
+/* Frees the flock's device memory (the cudaFree calls closing main,
+ * cuda/flock.cu:520-523). */
 void flk_close(flk_flock* f);
 
 /* ---- batched: many independent flocks, one launch per pass --------------- */
+/* No counterpart in the reference, whose backends run one flock per process
+ * (cuda/flock.cu:374-523). Each flock of a batch steps exactly as the plain
+ * step would step it alone; the calls below mirror the plain ones. */
 typedef struct flk_batch flk_batch;
 
+/* An empty batch on `device` (< 0: the current device); no counterpart. */
 int flk_batch_create(int32_t device, flk_batch** out);
-/* Adds a flock; *id receives its handle within the batch. */
+/* Adds a flock (as flk_open_host); *id receives its handle within the batch. */
 int flk_batch_add(flk_batch* b, uint32_t n, float time, const float* words, int32_t* id);
+/* Drops a flock and frees its storage for later flocks; no counterpart. */
 int flk_batch_remove(flk_batch* b, int32_t id);
 /* Advances every flock in the batch by `steps` steps (10-step CUDA graphs). */
 int flk_batch_step(flk_batch* b, uint32_t steps);
 /* Steps only the listed flocks, each by its own count (0 = idle). */
 int flk_batch_step_each(flk_batch* b, const int32_t* ids, const uint32_t* steps, uint32_t count);
+/* One flock's state, as flk_read_host (cuda/flock.cu:494-519). */
 int flk_batch_read(flk_batch* b, int32_t id, float* time, float* words);
 /* One step of every flock; per-flock grid/sets outputs concatenated in id
  * order of `ids` (same layouts as flk_step_debug, offsets per flock B_f+1). */
 int flk_batch_step_debug(flk_batch* b, const int32_t* ids, uint32_t count, uint32_t* keys, uint32_t* offsets,
                          uint32_t* sorted, uint32_t* sets);
-/* Launch shape: CTAs per SM of the streaming passes and decide, decide CTA
- * size, steps per captured graph. Zero keeps the current value. */
 /* flk_step_f64 for the listed flocks (one step each, the others idle):
  * `out64` (optional) receives each listed flock's FP64 post-step state
  * (n_f*15 doubles, bird order) concatenated in the order of `ids`; `reports`
  * (optional, 4 doubles per id) each flock's own error report, as flk_step_f64
  * gives it. A duplicated id is FLK_ERR_ARG. */
 int flk_batch_step_f64(flk_batch* b, const int32_t* ids, uint32_t count, double* out64, double* reports);
+/* Launch shape: CTAs per SM of the streaming passes and decide, decide CTA
+ * size, steps per captured graph. Zero keeps the current value. No
+ * counterpart: the reference fixes its launch shapes (cuda/flock.cu:453-470). */
 int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t decide_threads, int32_t graph_chunk);
 /* Chunk graphs instantiated, and updated in place (cudaGraphExecUpdate, when
  * only sizes or pointers changed, e.g. a flock joined or left), so far. */
 int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated);
+/* flk_counters summed over the batch's flocks. */
 int flk_batch_counters(flk_batch* b, uint64_t* due, uint64_t* candidates, uint64_t* pairs);
 /* Times `steps` graph-launched steps on the batch's stream with CUDA events. */
 int flk_batch_time_steps(flk_batch* b, uint32_t steps, double* ms);
 /* Every flock of the batch, `steps` eager steps with per-pass events; means of
  * the last steps-warmup steps (as flk_step_timed). */
 int flk_batch_step_timed(flk_batch* b, uint32_t steps, uint32_t warmup, flk_pass_times* out);
+/* Frees the batch and all its flocks (as flk_close). */
 void flk_batch_destroy(flk_batch* b);
 
 /* ---- served: continuous batching of simulate(flock, steps) requests ------ */
+/* No counterpart in the reference (one flock per process, cuda/flock.cu:374-523):
+ * requests arrive while others run, join the batched step at chunk boundaries
+ * and leave it when done; each result equals the plain step's alone. */
 typedef struct flk_pool flk_pool;
 
 typedef struct {
@@ -178,14 +193,19 @@ int flk_pool_error_report(flk_pool* p, uint64_t ticket, double* out64, double* r
 int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state);
 /* Blocks until done; *latency_ms = completion - submission (host clock). */
 int flk_pool_wait(flk_pool* p, uint64_t ticket, double* latency_ms);
+/* Counters since creation (the struct above). */
 int flk_pool_stats_get(flk_pool* p, flk_pool_stats* out);
+/* Stops the worker (requests still queued or resident fail) and frees the pool. */
 void flk_pool_destroy(flk_pool* p);
 
 /* ---- helpers -------------------------------------------------------------- */
+/* The calling thread's last error message: what the CK macro prints before
+ * exit(1) (cuda/flock.cu:27-34), returned instead. */
 const char* flk_last_error(void);
 /* Bird count and clock from a .flk header (state.rs:104-171). */
 int flk_file_info(const char* path, uint32_t* n, float* time);
-/* Canonical bucket count: next power of two >= 2n clamped to [2^16, 2^22]. */
+/* Canonical bucket count: next power of two >= 2n clamped to [2^16, 2^22]
+ * (cuda/flock.cu:368-372). */
 uint32_t flk_buckets_for(uint32_t n);
 /* The benchmark scatter (state.rs:79-101): n birds, SplitMix64 seed. */
 int flk_generate(uint32_t n, uint64_t seed, float* words);
@@ -194,12 +214,15 @@ int flk_generate(uint32_t n, uint64_t seed, float* words);
  * R_H, SIGMA, W_SEP, W_ALIGN, W_COH, BLIND_COS, W_ROOST_V, H_ROOST_V, Z0,
  * GRID_CELL, RADIUS_EXP (params.rs:5-65). Returns the count written. */
 int flk_params(float* out, int32_t cap);
-/* Device bytes a flock of n birds occupies when resident. */
+/* Device bytes a flock of n birds occupies when resident (the pool's admission
+ * unit); no counterpart. */
 uint64_t flk_bytes_for(uint32_t n);
-/* Engine kernel launches per step (for launch accounting). */
+/* Engine kernel launches per step (for launch accounting); the reference's
+ * step launches seven (cuda/flock.cu:453-470). */
 int flk_kernels_per_step(void);
 /* Page-locks / releases a caller's host buffer so state copies run at full
- * link speed (cudaHostRegister / cudaHostUnregister). */
+ * link speed (cudaHostRegister / cudaHostUnregister); no counterpart (the
+ * reference copies from pageable vectors, cuda/flock.cu:414-437). */
 int flk_pin(void* ptr, uint64_t bytes);
 int flk_unpin(void* ptr);
 
