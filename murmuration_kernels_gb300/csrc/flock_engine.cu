@@ -708,6 +708,15 @@ void Engine::run(uint32_t steps) {
     const uint32_t chunk = (uint32_t)std::max(1, shape_.graph_chunk);
     uint32_t done = 0;
     if (steps >= chunk) {
+        // A chunk graph that must be captured (first run, or the flock table
+        // changed) costs host time. With at least two chunks to run, the first
+        // chunk goes out as plain launches and the capture runs on the host
+        // while the GPU executes them; the launches are the captured ones, so
+        // the results are the same.
+        if (steps >= 2 * chunk && (!graph_ || graph_steps_ != chunk || graph_stale_)) {
+            enqueue_steps(chunk);
+            done = chunk;
+        }
         ensure_graph();
         device_ahead_ = true;
         for (; done + chunk <= steps; done += chunk) FLK_CUDA(cudaGraphLaunch(graph_, stream_));
