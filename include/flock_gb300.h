@@ -195,7 +195,9 @@ int flk_pool_poll(flk_pool* p, uint64_t ticket, int32_t* state);
 int flk_pool_wait(flk_pool* p, uint64_t ticket, double* latency_ms);
 /* Counters since creation (the struct above). */
 int flk_pool_stats_get(flk_pool* p, flk_pool_stats* out);
-/* Stops the worker (requests still queued or resident fail) and frees the pool. */
+/* Stops the worker and frees the pool. Results already being copied out land
+ * first; requests still queued or resident are dropped (their output buffers
+ * are not written). No other call on the pool may be in progress or follow. */
 void flk_pool_destroy(flk_pool* p);
 
 /* ---- helpers -------------------------------------------------------------- */
