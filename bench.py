@@ -510,7 +510,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (flock-ref gen scatter: SplitMix64, density 0.5)",
         "config": {"workload": f"plain single-flock step, {n:,} birds, seed {args.seed}", "birds": n,
                    "seed": args.seed, "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch"},
+                   "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch "
+                         "whose integrate counts the next step's grid, as in flk_step's multi-step runs"},
         "roofline": {"bound": "hbm", "kernel": "whole step (6 passes, one graph launch)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,

@@ -93,7 +93,10 @@ int flk_step_f64(flk_flock* f, double* out64, double* report);
  * passes inline, cuda/flock.cu:447-492): runs `steps` steps one graph launch
  * at a time; before each step it overwrites a `flush_bytes` device buffer so
  * the step starts with a cold L2, then brackets the step with CUDA events on
- * the library's stream. ms_per_step[steps] receives each step's device time. */
+ * the library's stream. ms_per_step[steps] receives each step's device time.
+ * Each step runs as in flk_step's multi-step runs: its integrate also counts
+ * the next step's grid. The first grid is counted before the first timed step
+ * and one untimed step follows the last, so the flock advances steps + 1. */
 int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step);
 /* Frees the flock's device memory (the cudaFree calls closing main,
  * cuda/flock.cu:520-523). */

@@ -296,7 +296,9 @@ class Flock:
         return a.value, b.value, c.value
 
     def time_steps(self, steps: int, flush_bytes: int = 256 << 20) -> np.ndarray:
-        """Device ms of each of `steps` single-step launches, L2 flushed before each."""
+        """Device ms of each of `steps` single-step launches, L2 flushed before each.
+        Each step counts the next step's grid as in step(); one untimed step
+        follows the last, so the flock advances steps + 1."""
         ms = np.zeros(steps, dtype=np.float32)
         _check(lib().flk_time_steps(self._h, steps, flush_bytes, _fptr(ms)))
         return ms

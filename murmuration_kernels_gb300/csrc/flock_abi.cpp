@@ -226,8 +226,9 @@ extern "C" int flk_counters(flk_flock* f, uint64_t* due, uint64_t* cand, uint64_
 
 extern "C" int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step) {
     if (!f || (steps && !ms_per_step)) return fail(FLK_ERR_ARG, "flk_time_steps: null pointer");
+    if (steps == UINT32_MAX) return fail(FLK_ERR_ARG, "flk_time_steps: too many steps");
     return guarded([&] {
-        f->eng->set_remaining({f->id}, {steps});
+        f->eng->set_remaining({f->id}, {steps + 1});  // the timed steps and one untimed step
         f->eng->time_steps_cold(steps, (size_t)flush_bytes, ms_per_step);
         return check_device(*f->eng);
     });

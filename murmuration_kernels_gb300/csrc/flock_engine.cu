@@ -476,31 +476,42 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     uint4* flush = nullptr;
     const size_t n16 = flush_bytes / 16;
     if (n16) FLK_CUDA(cudaMalloc(&flush, n16 * 16));
-    cudaGraph_t g;
-    cudaGraphExec_t one = nullptr;
-    FLK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(false);
-    FLK_CUDA(cudaStreamEndCapture(stream_, &g));
-    cudaError_t e = cudaGraphInstantiate(&one, g, 0);
-    cudaGraphDestroy(g);
-    FLK_CUDA(e);
+    // Each timed step is one launch of a single-step graph that runs the step as
+    // a multi-step run does: its integrate also counts the next step's grid, so
+    // the step has no hash pass of its own. Steps alternate between the two grid
+    // buffers, hence one graph per buffer. The first step's grid is counted
+    // before the timed region and one untimed step after it consumes the grid
+    // the last timed step counted: every timed step counts every bird once, and
+    // both grid buffers end clear.
+    cudaGraphExec_t one[2] = {nullptr, nullptr};
+    for (int b = 0; b < 2; ++b) {
+        cudaGraph_t g;
+        FLK_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(false, nullptr, false, b, false, true);
+        FLK_CUDA(cudaStreamEndCapture(stream_, &g));
+        cudaError_t e = cudaGraphInstantiate(&one[b], g, 0);
+        cudaGraphDestroy(g);
+        FLK_CUDA(e);
+    }
     std::vector<cudaEvent_t> ev(2 * (size_t)steps);
     for (auto& x : ev) FLK_CUDA(cudaEventCreate(&x));
-    device_ahead_ = true;
+    enqueue_hash(0);
     for (uint32_t s = 0; s < steps; ++s) {
         if (n16) k_flush<<<num_sms_ * 4, 256, 0, stream_>>>(flush, n16, s);
         FLK_CUDA(cudaEventRecord(ev[2 * s], stream_));
-        FLK_CUDA(cudaGraphLaunch(one, stream_));
+        FLK_CUDA(cudaGraphLaunch(one[s & 1u], stream_));
         FLK_CUDA(cudaEventRecord(ev[2 * s + 1], stream_));
     }
+    enqueue_step(false, nullptr, false, (int)(steps & 1u), false, false);
     FLK_CUDA(cudaGetLastError());
     FLK_CUDA(cudaStreamSynchronize(stream_));
     for (uint32_t s = 0; s < steps; ++s) FLK_CUDA(cudaEventElapsedTime(&ms_per_step[s], ev[2 * s], ev[2 * s + 1]));
     for (auto& x : ev) cudaEventDestroy(x);
-    cudaGraphExecDestroy(one);
+    for (auto& x : one) cudaGraphExecDestroy(x);
     if (flush) cudaFree(flush);
+    const uint32_t ran = steps + 1;
     for (size_t k = 0; k < table_h_.size(); ++k) {
-        const uint32_t left = table_h_[k].remaining > steps ? table_h_[k].remaining - steps : 0;
+        const uint32_t left = table_h_[k].remaining > ran ? table_h_[k].remaining - ran : 0;
         table_h_[k].remaining = left;
         if (table_ids_[k] >= 0) slots_[table_ids_[k]].remaining = left;
     }
@@ -625,7 +636,7 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
     if (sets)  // a grid-reporting step: the reference's cell hash
         k_hash_count<false><<<sgrid(fit_.hash[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
     else if (hash)
-        k_hash_count<true><<<sgrid(fit_.hash[1]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
+        enqueue_hash(buf);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
     if (sets) {
         // a step that reports its grid builds the canonical dense offsets
@@ -664,6 +675,13 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
         k_integrate<false><<<sgrid(fit_.integrate[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
     if (f64) k_compare_f64<<<sgrid(fit_.compare_f64), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
+}
+
+void Engine::enqueue_hash(int buf) {
+    device_ahead_ = true;
+    const int grid = pgrid(num_sms_, std::min(shape_.stream_blocks_per_sm, fit_.hash[1]), V_, 256);
+    k_hash_count<true><<<grid, 256, 0, stream_>>>(table_d_, (int)table_h_.size(), V_, ar_, key_, arrival_,
+                                                  grid_buf(buf), ctl_);
 }
 
 void Engine::enqueue_steps(uint32_t n) {

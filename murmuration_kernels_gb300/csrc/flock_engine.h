@@ -138,7 +138,10 @@ public:
     // run(steps) bracketed by CUDA events on the engine stream; returns ms.
     double time_run(uint32_t steps);
     // `steps` single-step graph launches, each after overwriting `flush_bytes`
-    // of device memory (cold L2), each bracketed by events; ms per step.
+    // of device memory (cold L2), each bracketed by events; ms per step. Each
+    // step runs as in a multi-step run (its integrate counts the next step's
+    // grid); one untimed step follows, so the flock advances steps + 1 and
+    // needs that many remaining.
     void time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_step);
     // Runs `steps` batched steps over the resident flocks (each flock stops
     // when its remaining count reaches zero). Uses captured CUDA graphs.
@@ -194,6 +197,8 @@ private:
     // `n` production steps, each integrate counting the next step's grid (the
     // first step counts its own, the last one counts none).
     void enqueue_steps(uint32_t n);
+    // The production hash and count of the current positions into grid buffer `buf`.
+    void enqueue_hash(int buf);
     GridBuf grid_buf(int k) const;
     void free_graphs();
     void destroy_graphs();

@@ -365,6 +365,26 @@ def test_graph_and_eager_launches_agree(native):
     assert a.read()[0] == b.read()[0]
 
 
+@pytest.mark.parametrize("k", [1, 4, 7])
+def test_cold_timed_steps_are_the_library_steps(native, k):
+    """flk_time_steps (the benchmark's timed steps: single-step graphs that count
+    the next step's grid, an L2 flush before each, one untimed step after) leaves
+    exactly the state that k + 1 steps of flk_step leave, and the library's next
+    steps continue from it as from the plain run."""
+    w = native.generate(50_000, 6)
+    a = native.Flock(w)
+    a.step(3)
+    ms = a.time_steps(k, 1 << 20)
+    assert ms.shape == (k,) and (ms > 0).all()
+    b = native.Flock(w)
+    b.step(3 + k + 1)
+    assert a.read()[1].tobytes() == b.read()[1].tobytes()
+    assert a.read()[0] == b.read()[0]
+    a.step(12)
+    b.step(12)
+    assert a.read()[1].tobytes() == b.read()[1].tobytes()
+
+
 def test_file_drop_in_and_cli(native, oracle, tmp_path):
     import subprocess
 
