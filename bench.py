@@ -512,7 +512,7 @@ def main():
                    "seed": args.seed, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch "
                          "whose integrate counts the next step's grid, as in flk_step's multi-step runs"},
-        "roofline": {"bound": "hbm", "kernel": "whole step (6 passes, one graph launch)",
+        "roofline": {"bound": "hbm", "kernel": "whole step (5 launches in one graph launch)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,
                      "traffic": traffic},
