@@ -111,3 +111,23 @@ def test_clock_summary_parses_nvidia_smi_rows(tmp_path):
     s = c.summary()
     assert s == {"sm_mhz": 2040.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
     assert not path.exists()
+
+
+def test_step_traffic_comes_from_the_committed_profile():
+    """roofline.traffic is the committed ncu figure for the 1M-bird step: the
+    summary's step_dram_bytes line, equal to its per-kernel table's sum."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    t = bench.step_traffic_bytes()
+    assert t is not None and t > 0
+    total = 0.0
+    for line in open(bench.TRAFFIC):
+        parts = line.split()
+        if not parts or not parts[0].startswith("k_") or len(parts) < 4:
+            continue
+        try:  # table rows: kernel, time, DRAM read MB, DRAM write MB, ...
+            total += (float(parts[2]) + float(parts[3])) * 1e6
+        except ValueError:
+            continue
+    assert abs(total - t) / t < 1e-3
