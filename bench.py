@@ -522,7 +522,10 @@ def main():
         "passes_ms": {k: round(v, 5) for k, v in r["passes"].items() if k.endswith("_ms")},
         "decide": decide_rates(r, n),
         "passes_gbs": pass_bandwidths(r, n),
-        "gpu_launches": m.kernels_per_step() * K,
+        # a timed step has no hash pass of its own (the previous integrate counted its grid)
+        "gpu_launches": (m.kernels_per_step() - 1) * K,
+        "gpu_launches_how": "kernels in the timed steps' graph launches: place, scatter, sort, decide and "
+                            "integrate per step (the L2-flush kernel between steps not counted)",
         "fp64_error": dict(r["fp64"], how="one more f32 step against the same step in FP64 from the same state "
                                           "(max relative position / velocity error over all birds; neighbour-count "
                                           "mismatches)"),
