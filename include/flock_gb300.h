@@ -240,13 +240,14 @@ int flk_unpin(void* ptr);
  * stable sorted[n] that flk_step_debug reports -- from n positions
  * pos4[4n] (x, y, z, unused) in device memory into caller-owned device
  * buffers (pos4 and offsets 16-byte aligned), on `stream` (a cudaStream_t,
- * NULL = legacy default stream), and
- * synchronises that stream before returning. It calls no allocator: its
+ * NULL = legacy default stream). It is a blocking call: it synchronises that
+ * stream before returning. It calls no allocator: its
  * scratch is one fixed device array inside the library (about 2.5 MiB, held on
  * every GPU that loads the library until exit), sized for at most
- * FLK_NOALLOC_MAX_BIRDS birds; larger n returns FLK_ERR_CAPACITY. The first call
- * on each device looks up that array's device address, so make it before any
- * stream capture. Calls share the array: concurrent calls on one device race. */
+ * FLK_NOALLOC_MAX_BIRDS birds; larger n returns FLK_ERR_CAPACITY. Each call
+ * looks up that array's device address on the current device. n = 0 still
+ * writes all buckets_for(0)+1 = 65,537 offsets (zeros). Calls share the array:
+ * concurrent calls on one device race. */
 #define FLK_NOALLOC_MAX_BIRDS 131072u
 int flk_grid_noalloc(const float* pos4, uint32_t n, uint32_t* keys, uint32_t* offsets, uint32_t* sorted, void* stream);
 

@@ -14,10 +14,11 @@
 // array (about 2.5 MiB) until the process exits.
 //
 // The array's name in host code is only a host-side handle, not a device
-// address, so the host looks the address up with cudaGetSymbolAddress once per
-// device (with that device current) on the first call made on that device, and
-// passes the pointer to the kernels. Make that first call on a device before
-// any stream capture starts.
+// address, so every call looks the address up with cudaGetSymbolAddress on the
+// current device and passes the pointer to the kernels. Nothing is cached
+// across calls, so a device reset between calls (which reloads the module and
+// moves the array) cannot leave a stale address behind. The call is blocking:
+// it synchronises its stream before it returns.
 //
 // All calls share the one array and it keeps the previous call's contents:
 // each call clears the parts that must start at zero. Calls that overlap on the
@@ -32,7 +33,6 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/flock_gb300.h"
@@ -271,9 +271,6 @@ __global__ void k_na_segsort(const uint32_t* __restrict__ offsets, uint32_t n, u
     }
 }
 
-std::mutex g_setup_mu;
-unsigned char* g_scratch_ptr[256] = {nullptr};  // device address of the array, per device ordinal
-
 int na_fail(int code, const std::string& m) {
     flk::set_last_error(m);  // reported by flk_last_error()
     return code;
@@ -291,23 +288,12 @@ extern "C" int flk_grid_noalloc(const float* pos4, uint32_t n, uint32_t* keys, u
     // float4 loads of pos4 and 16-byte stores into offsets need 16-byte alignment
     if ((reinterpret_cast<uintptr_t>(pos4) | reinterpret_cast<uintptr_t>(offsets)) & 15u)
         return na_fail(FLK_ERR_ARG, "flk_grid_noalloc: pos4 and offsets must be 16-byte aligned");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return na_fail(FLK_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 256) return na_fail(FLK_ERR_ARG, "flk_grid_noalloc: device ordinal out of range");
-    unsigned char* base = nullptr;
-    {
-        // set-up, once per device, with that device current
-        std::lock_guard<std::mutex> lk(g_setup_mu);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_flk_noalloc_scratch);
-            if (e != cudaSuccess)
-                return na_fail(FLK_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-        }
-        base = g_scratch_ptr[dev];
-    }
+    // the scratch array's device address on the current device, looked up on
+    // every call (cheap next to the stream synchronisation below)
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_flk_noalloc_scratch);
+    if (e != cudaSuccess) return na_fail(FLK_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    unsigned char* base = static_cast<unsigned char*>(p);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint64_t want = 1;
     while (want < (uint64_t)n * 2) want <<= 1;

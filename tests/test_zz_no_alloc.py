@@ -29,6 +29,7 @@ class DeviceBuffers:
         self._ck(self.cu.cuInit(0))
         dev = C.c_int()
         self._ck(self.cu.cuDeviceGet(C.byref(dev), 0))
+        self.dev = dev
         self.ctx = C.c_void_p()
         self._ck(self.cu.cuDevicePrimaryCtxRetain(C.byref(self.ctx), dev))
         self._ck(self.cu.cuCtxSetCurrent(self.ctx))
@@ -58,6 +59,10 @@ class DeviceBuffers:
         for p in self.ptrs:
             self.cu.cuMemFree_v2(C.c_uint64(p))
         self.ptrs = []
+        if self.ctx:
+            # balances the retain above (the runtime holds its own reference)
+            self.cu.cuDevicePrimaryCtxRelease_v2(self.dev)
+            self.ctx = None
 
 
 def grid_noalloc(native, bufs, words):
@@ -88,6 +93,25 @@ def test_grid_noalloc_equals_flk_step_debug_on_two_calls_in_a_row(native):
             assert np.array_equal(keys, want["keys"]), n
             assert np.array_equal(offs, want["offsets"]), n
             assert np.array_equal(srt, want["sorted"]), n
+    finally:
+        bufs.free()
+
+
+def test_grid_noalloc_of_an_empty_flock_writes_every_offset(native):
+    # n = 0 still has buckets_for(0) = 65,536 buckets: all 65,537 offsets are written as 0
+    bufs = DeviceBuffers()
+    try:
+        B = native.buckets_for(0)
+        assert B == 1 << 16
+        L = native.lib()
+        fn = L.flk_grid_noalloc
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
+        d_offs = bufs.upload(np.full(B + 1, 0xDEADBEEF, dtype=np.uint32))
+        d_pos = bufs.alloc(16)
+        rc = fn(d_pos, 0, 0, d_offs, 0, None)
+        assert rc == 0, L.flk_last_error()
+        assert np.array_equal(bufs.download(d_offs, B + 1), np.zeros(B + 1, dtype=np.uint32))
     finally:
         bufs.free()
 
