@@ -201,7 +201,7 @@ def cpu_sample(words: np.ndarray, budget_s: float, seed: int = 0) -> dict:
     return {"value": n / step_s, "unit": "bird-updates/s", "cores": threads, "kind": "port",
             "sample": f"brute-force decide of {m} of the {len(due)} deciding birds (each against all {n}) "
                       f"+ integrate of all {n}; extrapolated to one step ({step_s:.3f} s)",
-            "sample_wall_s": round(t_dec + t_int, 3)}
+            "sample_wall_s": round(t_dec + t_int, 3), "extrapolated_step_s": step_s}
 
 
 def cpu_grid_steps(words: np.ndarray, steps: int) -> dict:
@@ -221,7 +221,24 @@ def cpu_grid_steps(words: np.ndarray, steps: int) -> dict:
                       f"cuda/flock.cu's decide), {wall:.2f} s"}
 
 
+def workload_config(n: int, seed: int, world: int) -> dict:
+    """The `config` of both arms' lines (the same dict, so the arms compare)."""
+    return {"workload": f"plain single-flock step, {n:,} birds, seed {seed}", "birds": n, "seed": seed,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch "
+                  "whose integrate counts the next step's grid, as in flk_step's multi-step runs"}
+
+
 def run_reference(args, dist, rank):
+    """The reference's CPU step (its brute-force flock-ref oracle, restated in C)
+    on all host cores. A full step at 1M birds takes ~24 s of CPU, so each
+    step here is a bounded sample of one: the brute-force decide of a random
+    subset of that step's deciding birds, plus integrate of every bird. The
+    line reports what ran: `ms_per_step` is the measured wall time of one
+    sampled step, and `value` is the rate of the work it did, in bird-update
+    equivalents per second (the sample's fraction of a full step's work x n,
+    over its wall time), which equals n over the extrapolated full-step time
+    (`extrapolated_step_s`)."""
     if rank != 0:
         return
     from oracle import pyoracle as o
@@ -230,22 +247,53 @@ def run_reference(args, dist, rank):
     per_step = max(0.05, 90.0 / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
         cpu_sample(words, 0.02)
-    vals, walls = [], []
+    walls, steps_s, fracs = [], [], []
     for s in range(args.steps):
         r = cpu_sample(words, per_step, seed=s)
-        vals.append(r["value"])
         walls.append(r["sample_wall_s"])
-    step_s = statistics.mean(args.birds / v for v in vals)
-    value = args.birds / step_s
+        steps_s.append(r["extrapolated_step_s"])
+        fracs.append(r["sample_wall_s"] / r["extrapolated_step_s"])
+    ext = statistics.mean(steps_s)
+    value = args.birds / ext
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     out = {"metric": METRIC, "impl": "reference", "value": value, "unit": "bird-updates/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (flock-ref gen scatter)",
-           "config": {"workload": f"plain single-flock step, {args.birds:,} birds, seed {args.seed}",
-                      "birds": args.birds, "seed": args.seed},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (flock-ref gen scatter: SplitMix64, density 0.5)",
+           "config": workload_config(args.birds, args.seed, world),
+           "extrapolated_step_s": ext, "work_fraction_per_step": statistics.mean(fracs),
+           "how": "each timed step is a bounded sample of one full step (the brute-force decide of a random subset "
+                  "of its deciding birds, each against all birds, plus integrate of every bird); ms_per_step is "
+                  "that sample's measured wall time; value = the sample's share of a full step's work x birds / "
+                  "its wall time = birds / extrapolated_step_s",
            "cpu_baseline": {"value": value, "unit": "bird-updates/s", "cores": r["cores"], "kind": "port",
-                            "sample": f"per step: {r['sample']}; mean over {args.steps} steps"},
+                            "sample": f"per step: {r['sample']}; {args.steps} sampled steps"},
            "e2e": {"value": value, "unit": "bird-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def ref_gpu(n: int, seed: int, steps: int, warmup: int, device: int, words=None) -> dict:
+    """Reported baseline, not our product: the reference's own CUDA kernels
+    (cuda/flock.cu compiled unchanged for sm_103a, oracle/_ref) on this GPU,
+    driven with the reference's host loop and per-pass timing protocol
+    (cuda/flock.cu:447-492), on the same starting state."""
+    try:
+        from oracle import ref_kernels as rk
+
+        drv = rk.Driver(device)
+        try:
+            t = rk.time_reference(drv, n, seed, steps, warmup, words=words)
+        finally:
+            drv.close()
+    except Exception as e:  # the cubin is built only where the reference is mounted
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    return {"kind": "reference kernels (cuda/flock.cu for sm_103a, same GPU)", "birds": n, "seed": seed,
+            "steps": steps, "warmup": warmup, "value": t["bird_steps_per_s"], "unit": "bird-updates/s",
+            "ms_per_step": t["step_total"],
+            "passes_ms": {k: round(t[k], 5) for k in ("grid_histogram", "grid_scan", "grid_scatter", "decide",
+                                                      "integrate")},
+            "how": "memset + 7 launches per step on one stream, CUDA events between passes, mean GPU ms per pass "
+                   "over the timed steps (the reference's own protocol; no L2 flush)"}
 
 
 # ---------------------------------------------------------------------------
@@ -298,8 +346,12 @@ def pass_bandwidths(r, n):
 
 
 # decide's warp instructions per launch at 1M birds (seed 1), from the committed
-# ncu summary (smsp__inst_executed.sum); 4 warp instructions per clock per SM peak
+# ncu summary (smsp__inst_executed.sum) of the decide kernel as of commit
+# PROFILED_AT; 4 warp instructions per clock per SM peak. Both this figure and
+# the step traffic in profiles/traffic_step_1m.txt are re-taken whenever the
+# kernels change.
 DECIDE_INST_1M = 122.1e6
+PROFILED_AT = "cc967b2"
 GB300_SMS = 152
 
 
@@ -317,8 +369,38 @@ def dominant_kernel(r, n, seed):
         achieved = DECIDE_INST_1M / (p["decide_ms"] / 1e3)
         peak = 4.0 * GB300_SMS * mhz * 1e6
         out.update({"issue_achieved": achieved, "issue_peak": peak, "issue_unit": "warp instructions/s",
-                    "issue_frac": achieved / peak})
+                    "issue_frac": achieved / peak,
+                    "instructions_source": f"{DECIDE_INST_1M:.4g} warp instructions per launch from "
+                                           f"profiles/decide_1m_current.txt (profiled at commit {PROFILED_AT}) "
+                                           f"over this run's decide time"})
     return out
+
+
+def bench_configs(m, local) -> list:
+    """The plain step at the other two single-flock sizes, each with its own
+    steps protocol: 100,000 birds (seed 1, 20 warm-up + 20 timed) and
+    16,777,216 birds (seed 7, 10 + 50). Timed as the headline (one graph
+    launch per step after an L2 flush, CUDA events), beside the reference's
+    kernels on the same GPU and the same starting state."""
+    rows = []
+    for n, seed, warm, steps in [(100_000, 1, 20, 20), (16_777_216, 7, 10, 50)]:
+        words = m.generate(n, seed)
+        f = m.Flock(words, 0.0, device=local)
+        f.step(warm)
+        with ClockSampler(local) as clk:
+            ms = f.time_steps(steps, FLUSH_BYTES)
+        f.close()
+        v = n * steps / (float(ms.sum()) / 1e3)
+        ref = ref_gpu(n, seed, warm + steps, warm, local, words=words)
+        row = {"workload": f"plain single-flock step, {n:,} birds, seed {seed}", "birds": n, "seed": seed,
+               "warmup": warm, "steps": steps, "value": v, "unit": "bird-updates/s",
+               "ms_per_step": float(ms.mean()), "step_ms_p50": float(np.median(ms)), "clocks": clk.summary(),
+               "ref_gpu": ref}
+        if "value" in ref:
+            row["speedup_vs_ref_gpu"] = v / ref["value"]
+        rows.append(row)
+        del words
+    return rows
 
 
 def bench_multi_step(m, args, local):
@@ -508,14 +590,13 @@ def main():
         "metric": METRIC, "value": value, "unit": "bird-updates/s", "n_gpus": world, "steps": K,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (flock-ref gen scatter: SplitMix64, density 0.5)",
-        "config": {"workload": f"plain single-flock step, {n:,} birds, seed {args.seed}", "birds": n,
-                   "seed": args.seed, "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "flushed before every timed step (256 MB write); each step one CUDA-graph launch "
-                         "whose integrate counts the next step's grid, as in flk_step's multi-step runs"},
+        "config": workload_config(n, args.seed, world),
         "roofline": {"bound": "hbm", "kernel": "whole step (5 launches in one graph launch)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "bytes_per_update": b_alg, "due_fraction": f,
-                     "traffic": traffic},
+                     "traffic": traffic,
+                     "traffic_source": f"{os.path.relpath(TRAFFIC, ROOT)} (ncu capture of one timed step; "
+                                       f"profiled at commit {PROFILED_AT})" if traffic else None},
         # what bounds the step: decide's share of the eager pass times (live) and its
         # limiter, from the committed ncu summary of the same workload
         "dominant_kernel": dominant_kernel(r, n, args.seed),
@@ -535,6 +616,13 @@ def main():
     if rank == 0:
         out["e2e"] = bench_e2e(m, args, local)
         out["multi_step"] = bench_multi_step(m, args, local)
+        # the reference's own kernels on this GPU at the headline workload, with
+        # the reference's protocol for it (20 warm-up + 100 timed steps)
+        out["ref_gpu"] = ref_gpu(n, args.seed, 120, 20, local, words=m.generate(n, args.seed))
+        if "value" in out["ref_gpu"]:
+            out["ref_gpu"]["speedup"] = value / out["ref_gpu"]["value"]
+        if not args.no_extra:
+            out["configs"] = bench_configs(m, local)
         if not args.no_extra:
             out["batched"] = bench_batched(m, args, local)
             out["served"] = bench_served(m, args, local)

@@ -68,6 +68,15 @@ int flk_read_host(flk_flock* f, float* time, float* words);
 int flk_write_file(flk_flock* f, const char* path);
 /* Bird count and canonical bucket count (cuda/flock.cu:368-372). */
 int flk_size(const flk_flock* f, uint32_t* n, uint32_t* buckets);
+/* The reference's decide occupancy experiment (--decide-smem N and the
+ * "# decide occupancy" line, cuda/flock.cu:377,385,440-445): reserves
+ * `extra_smem` bytes of dynamic shared memory per decide CTA beyond what
+ * decide uses itself (0 = none), for every later step of this flock, and
+ * reports the resulting launch: resident CTAs per SM, threads per CTA, the
+ * SM's thread limit and the CTA's dynamic shared memory in bytes. Any output
+ * may be NULL. A reservation no CTA can hold is FLK_ERR_ARG. */
+int flk_decide_occupancy(flk_flock* f, uint64_t extra_smem, int32_t* blocks_per_sm, int32_t* threads,
+                         int32_t* threads_per_sm, uint64_t* smem_bytes);
 /* Runs ONE step and returns the grid it built and the neighbour-set summary
  * of every deciding bird, for bit-exact parity checks:
  *   keys[n]          bucket of each bird (cuda/flock.cu:118-124 grid_histogram)
@@ -202,6 +211,21 @@ int flk_pool_stats_get(flk_pool* p, flk_pool_stats* out);
  * first; requests still queued or resident are dropped (their output buffers
  * are not written). No other call on the pool may be in progress or follow. */
 void flk_pool_destroy(flk_pool* p);
+
+/* ---- failure paths ------------------------------------------------------- */
+/* Text for a device error word (what FLK_ERR_DEVICE's message reports):
+ * 1 = a scan look-back wait gave up, 2 = a bucket range or slot fell outside
+ * its array and was skipped. The reference has no device error word: its CK
+ * macro prints and exits (cuda/flock.cu:27-34). */
+const char* flk_device_error_text(uint32_t word);
+/* Test hook for the bounded device waits; no counterpart. Arms the flock's
+ * NEXT grid-reporting step (flk_step_debug): scan tile `skip_tile` publishes
+ * no look-back flag, so the tiles after it wait for a flag nothing sets, and
+ * every look-back gives up after `spin_limit` polls (0 keeps the usual limit
+ * of 2^22). That step returns FLK_ERR_DEVICE with the scan-timeout text and
+ * leaves the flock's state unusable (close it); the device and the process
+ * stay usable. No fault, trap or unbounded wait is involved. */
+int flk_debug_scan_timeout(flk_flock* f, uint32_t skip_tile, uint32_t spin_limit);
 
 /* ---- helpers -------------------------------------------------------------- */
 /* The calling thread's last error message: what the CK macro prints before

@@ -73,6 +73,9 @@ _SIGS = {
     "flk_read_host": (C.c_int, [_P, _PF, _PF]),
     "flk_write_file": (C.c_int, [_P, C.c_char_p]),
     "flk_size": (C.c_int, [_P, _PU, _PU]),
+    "flk_decide_occupancy": (C.c_int, [_P, C.c_uint64, _PI, _PI, _PI, _PU64]),
+    "flk_device_error_text": (C.c_char_p, [C.c_uint32]),
+    "flk_debug_scan_timeout": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "flk_step_debug": (C.c_int, [_P, _PU, _PU, _PU, _PU]),
     "flk_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
     "flk_step_f64": (C.c_int, [_P, _PD, _PD]),
@@ -193,6 +196,11 @@ def file_info(path: str) -> tuple[int, float]:
     return n.value, t.value
 
 
+def device_error_text(word: int) -> str:
+    """What a device error word means (the text FLK_ERR_DEVICE reports)."""
+    return lib().flk_device_error_text(word).decode()
+
+
 def buckets_for(n: int) -> int:
     return int(lib().flk_buckets_for(n))
 
@@ -294,6 +302,19 @@ class Flock:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().flk_counters(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def decide_occupancy(self, extra_smem: int = 0) -> dict[str, int]:
+        """Reserves `extra_smem` more bytes of shared memory per decide CTA (the
+        reference's --decide-smem) and returns decide's launch occupancy."""
+        bps, th, tpsm, sm = C.c_int32(), C.c_int32(), C.c_int32(), C.c_uint64()
+        _check(lib().flk_decide_occupancy(self._h, extra_smem, C.byref(bps), C.byref(th), C.byref(tpsm),
+                                          C.byref(sm)))
+        return {"blocks_per_sm": bps.value, "threads": th.value, "threads_per_sm": tpsm.value,
+                "smem_bytes": sm.value}
+
+    def debug_scan_timeout(self, skip_tile: int = 0, spin_limit: int = 1000) -> None:
+        """Test hook: the next step_debug's scan gives up waiting (FLK_ERR_DEVICE)."""
+        _check(lib().flk_debug_scan_timeout(self._h, skip_tile, spin_limit))
 
     def time_steps(self, steps: int, flush_bytes: int = 256 << 20) -> np.ndarray:
         """Device ms of each of `steps` single-step launches, L2 flushed before each.

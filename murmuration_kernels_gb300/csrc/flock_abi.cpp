@@ -50,8 +50,7 @@ int guarded(F&& f) {
 
 int check_device(Engine& e) {
     const uint32_t err = e.check_device_error();
-    if (err == flk::DEV_SCAN_TIMEOUT) return fail(FLK_ERR_DEVICE, "device: a scan look-back wait gave up");
-    if (err) return fail(FLK_ERR_DEVICE, "device error word " + std::to_string(err));
+    if (err) return fail(FLK_ERR_DEVICE, std::string("device: ") + flk_device_error_text(err));
     return FLK_OK;
 }
 
@@ -170,6 +169,36 @@ extern "C" int flk_write_file(flk_flock* f, const char* path) {
     int rc = flk_read_host(f, &time, w.data());
     if (rc) return rc;
     return write_flk(path, time, w.data(), f->n);
+}
+
+extern "C" int flk_decide_occupancy(flk_flock* f, uint64_t extra_smem, int32_t* blocks_per_sm, int32_t* threads,
+                                    int32_t* threads_per_sm, uint64_t* smem_bytes) {
+    if (!f) return fail(FLK_ERR_ARG, "flk_decide_occupancy: null handle");
+    return guarded([&] {
+        flk::LaunchShape s = f->eng->shape();
+        s.decide_extra_smem = (size_t)extra_smem;
+        f->eng->set_shape(s);  // rejects a reservation no CTA can hold
+        int bps = 0, th = 0, tpsm = 0;
+        size_t smem = 0;
+        f->eng->decide_occupancy(&bps, &th, &smem);
+        const cudaError_t e = cudaDeviceGetAttribute(&tpsm, cudaDevAttrMaxThreadsPerMultiProcessor, f->eng->device());
+        if (e != cudaSuccess) return fail(FLK_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+        if (blocks_per_sm) *blocks_per_sm = bps;
+        if (threads) *threads = th;
+        if (threads_per_sm) *threads_per_sm = tpsm;
+        if (smem_bytes) *smem_bytes = smem;
+        return FLK_OK;
+    });
+}
+
+extern "C" const char* flk_device_error_text(uint32_t word) { return flk::device_error_text(word); }
+
+extern "C" int flk_debug_scan_timeout(flk_flock* f, uint32_t skip_tile, uint32_t spin_limit) {
+    if (!f) return fail(FLK_ERR_ARG, "flk_debug_scan_timeout: null handle");
+    return guarded([&] {
+        f->eng->arm_scan_timeout(skip_tile, spin_limit);
+        return FLK_OK;
+    });
 }
 
 extern "C" int flk_size(const flk_flock* f, uint32_t* n, uint32_t* buckets) {

@@ -61,6 +61,15 @@ namespace flk {
         }                                                                                                 \
     } while (0)
 
+const char* device_error_text(uint32_t word) {
+    switch (word) {
+        case DEV_OK: return "no device error";
+        case DEV_SCAN_TIMEOUT: return "a scan look-back wait gave up (error word 1)";
+        case DEV_BAD_RANGE: return "a bucket range or slot fell outside its array and was skipped (error word 2)";
+        default: return "unknown device error word";
+    }
+}
+
 uint32_t buckets_for(uint32_t n) {
     uint64_t want = 1;
     while (want < (uint64_t)n * 2) want <<= 1;
@@ -143,14 +152,35 @@ size_t Engine::bytes_for(uint32_t n) {
     return (size_t)n * (136 + 88) + b * 16 + (b / SCAN_TILE) * 8 + 256;
 }
 
+size_t Engine::decide_smem(bool sets) const {
+    const size_t w = (size_t)(shape_.decide_threads / 32);
+    return w * (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>()) + shape_.decide_extra_smem;
+}
+
+void Engine::decide_occupancy(int* blocks_per_sm, int* threads, size_t* smem_bytes) const {
+    const size_t smem = decide_smem(false);
+    int n = 0;
+    FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decide<false>, shape_.decide_threads, smem));
+    *blocks_per_sm = n;
+    *threads = shape_.decide_threads;
+    *smem_bytes = smem;
+}
+
 void Engine::set_shape(const LaunchShape& s) {
+    int optin = 0;
+    FLK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+    const size_t w = (size_t)(s.decide_threads / 32);
+    const size_t need = std::max(w * decide_smem_per_warp<false>(), w * decide_smem_per_warp<true>()) +
+                        s.decide_extra_smem;
+    if (need > (size_t)optin)
+        throw Error{-1, "decide would need " + std::to_string(need) + " B of shared memory per CTA, above the " +
+                            std::to_string(optin) + " B a CTA may have"};
     shape_ = s;
     // decide's dynamic shared memory grows with its CTA size; allow past 48 KB
-    const int w = s.decide_threads / 32;
     FLK_CUDA(cudaFuncSetAttribute(k_decide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(w * decide_smem_per_warp<false>())));
+                                  (int)decide_smem(false)));
     FLK_CUDA(cudaFuncSetAttribute(k_decide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(w * decide_smem_per_warp<true>())));
+                                  (int)decide_smem(true)));
     auto fit = [](auto kernel) {
         int n = 0;
         FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0));
@@ -657,9 +687,8 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
     const int dblocks = pgrid(num_sms_, shape_.decide_blocks_per_sm, V_, shape_.decide_threads / 32);
-    // per-warp hit queue + reduced birds awaiting their epilogue
-    const size_t qbytes = (size_t)(shape_.decide_threads / 32) *
-                          (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>());
+    // per-warp hit queue + reduced birds awaiting their epilogue (+ any reserved extra)
+    const size_t qbytes = decide_smem(sets);
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                        g.counts, ar_, sfwd_, radius_table_, sets_,
@@ -799,6 +828,12 @@ void Engine::step_debug(std::vector<GridDebug>* out) {
     enqueue_step(true);
     FLK_CUDA(cudaGetLastError());
     FLK_CUDA(cudaStreamSynchronize(stream_));
+    // a grid the device gave up on is not interpreted
+    if (const uint32_t err = check_device_error()) {
+        table_dirty_ = true;
+        device_ahead_ = true;
+        throw Error{-6, std::string("device: ") + device_error_text(err)};
+    }
     std::vector<uint32_t> key(V_), offs((size_t)Btot_ + 1), sets((size_t)V_ * 8);
     FLK_CUDA(cudaMemcpy(key.data(), key_, (size_t)V_ * 4, cudaMemcpyDeviceToHost));
     FLK_CUDA(cudaMemcpy(offs.data(), offsets_, ((size_t)Btot_ + 1) * 4, cudaMemcpyDeviceToHost));
@@ -916,6 +951,13 @@ uint32_t Engine::check_device_error() {
         FLK_CUDA(cudaStreamSynchronize(stream_));
     }
     return c.error;
+}
+
+void Engine::arm_scan_timeout(uint32_t skip_tile, uint32_t spin_limit) {
+    FLK_CUDA(cudaSetDevice(device_));
+    const uint32_t v[2] = {skip_tile + 1u, spin_limit};
+    FLK_CUDA(cudaMemcpyAsync(&ctl_->scan_skip1, v, sizeof v, cudaMemcpyHostToDevice, stream_));
+    FLK_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void Engine::counters(unsigned long long* due, unsigned long long* cand, unsigned long long* pairs) {

@@ -58,7 +58,12 @@ struct StepCtl {
     unsigned long long due_total;   // cumulative deciding birds
     unsigned long long cand_total;  // cumulative candidate tests in decide
     unsigned long long pair_total;  // cumulative pairs inside 2R
-    unsigned long long pad2;
+    // Test hook, one step only (the next grid-reporting step's scan; integrate's
+    // last block clears both): scan tile scan_skip1 - 1 publishes no status
+    // flag (0 = none), so the tiles after it wait for a flag nothing sets;
+    // scan_spin, if non-zero, replaces the look-back's poll limit.
+    uint32_t scan_skip1;
+    uint32_t scan_spin;
 };
 
 // One of the two grid buffers: the histogram (run lengths, per bucket), the
@@ -99,6 +104,7 @@ struct LaunchShape {
     int decide_blocks_per_sm = 1;   // decide CTAs per SM
     int segsort_blocks_per_sm = 8;  // segment-sort CTAs per SM (256 threads)
     int graph_chunk = 10;           // steps per captured CUDA graph
+    size_t decide_extra_smem = 0;   // dynamic shared memory reserved beyond decide's own (occupancy experiments)
 };
 
 struct GridDebug {  // host copies of one step's grid and neighbour-set summaries
@@ -159,12 +165,22 @@ public:
     void step_f64(std::vector<std::vector<double>>* out, std::vector<std::array<double, 4>>* report);
     void sync();
     uint32_t check_device_error();  // returns and clears the device error word
+    // Test hook for the bounded device waits: in the next grid-reporting step,
+    // scan tile `skip_tile` publishes no look-back flag and every look-back
+    // gives up after `spin_limit` polls (0: the usual limit). The step then
+    // ends with the device error word set to DEV_SCAN_TIMEOUT.
+    void arm_scan_timeout(uint32_t skip_tile, uint32_t spin_limit);
 
     cudaStream_t stream() const { return stream_; }
     int device() const { return device_; }
     int num_sms() const { return num_sms_; }
     LaunchShape& shape() { return shape_; }
     void set_shape(const LaunchShape& s);
+    // decide's launch as configured: resident CTAs per SM, threads per CTA and
+    // dynamic shared memory per CTA (bytes), for production steps
+    void decide_occupancy(int* blocks_per_sm, int* threads, size_t* smem_bytes) const;
+    // decide's dynamic shared memory per CTA for a step kind (its own + the reserved extra)
+    size_t decide_smem(bool sets) const;
     size_t device_bytes() const { return dev_bytes_; }
     // Cumulative counters from the step-control block.
     void counters(unsigned long long* due, unsigned long long* cand, unsigned long long* pairs);
@@ -267,6 +283,9 @@ private:
 uint32_t buckets_for(uint32_t n);
 // Bucket count of a production step (the same rule without the 2^22 clamp).
 uint32_t production_buckets(uint32_t n);
+
+// What a device error word (DeviceError) means, as FLK_ERR_DEVICE reports it.
+const char* device_error_text(uint32_t word);
 
 // Device-error and CUDA failures surface as this exception inside the library;
 // the C ABI turns it into a status code and a message.

@@ -164,6 +164,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
     }
     const uint32_t epoch = *(volatile uint32_t*)&ctl->epoch & 0x3FFFFFFFu;
     const size_t base = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+    // test hook (normally 0 / 0): a tile that publishes nothing, a shorter poll limit
+    const bool publish = tile + 1u != *(volatile uint32_t*)&ctl->scan_skip1;
+    const uint32_t spin = *(volatile uint32_t*)&ctl->scan_spin;
+    const uint32_t spin_limit = spin ? spin : SCAN_SPIN_LIMIT;
 
     uint4 c[SCAN_ITEMS / 4];
     const uint4* src = reinterpret_cast<const uint4*>(counts + base);
@@ -194,9 +198,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
     if (warp == 0) {
         uint32_t excl = 0;
         if (tile == 0) {
-            if (lane == 0) st_relaxed(&status[0], scan_word(epoch, FLAG_P, agg));
+            if (lane == 0 && publish) st_relaxed(&status[0], scan_word(epoch, FLAG_P, agg));
         } else {
-            if (lane == 0) st_relaxed(&status[tile], scan_word(epoch, FLAG_A, agg));
+            if (lane == 0 && publish) st_relaxed(&status[tile], scan_word(epoch, FLAG_A, agg));
             int pred = (int)tile - 1;
             uint32_t polls = 0;
             while (true) {
@@ -210,7 +214,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
                         val = (uint32_t)w;
                     }
                     if (__all_sync(FULL, flag != 0)) break;
-                    if (++polls > SCAN_SPIN_LIMIT) {  // give up: record and let every waiter finish
+                    if (++polls > spin_limit) {  // give up: record and let every waiter finish
                         if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_SCAN_TIMEOUT);
                         flag = FLAG_P;
                         val = 0;
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const uint32_t* __restric
                 if (pm) break;
                 pred -= 32;
             }
-            if (lane == 0) st_relaxed(&status[tile], scan_word(epoch, FLAG_P, excl + agg));
+            if (lane == 0 && publish) st_relaxed(&status[tile], scan_word(epoch, FLAG_P, excl + agg));
         }
         if (lane == 0) s_prefix = excl;
     }
@@ -453,6 +457,10 @@ __device__ __forceinline__ void emit_sorted(bool has, uint32_t pos, unsigned lon
     uint32_t nst = 0;
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), c = a;
     f3 fw = mk(0.f, 0.f, 0.f);
+    if (has && ((uint32_t)x & 0x7FFFFFFFu) >= d.n) {  // never with a consistent grid
+        atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);
+        has = false;
+    }
     if (has) {
         const uint32_t bird = (uint32_t)(x >> 31) & 0x7FFFFFFFu;
         const uint32_t ost = d.vbase + ((uint32_t)x & 0x7FFFFFFFu) + oshift;

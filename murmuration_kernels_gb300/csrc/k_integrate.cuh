@@ -110,6 +110,8 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
             *cur.occ_count = 0;
             ctl->due_count = 0;
             ctl->scan_ticket = 0;
+            ctl->scan_skip1 = 0;  // the scan test hook lasts one step
+            ctl->scan_spin = 0;
             ctl->epoch = ctl->epoch + 1;
             ctl->done_blocks = 0;
         }

@@ -127,3 +127,11 @@ def test_header_is_plain_c(native, tmp_path):
         r = subprocess.run([cc, *extra, "-Wall", "-Wextra", "-I" + hdr_dir, "-c", str(src), "-o",
                             str(tmp_path / "use.o")], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_device_error_words_map_to_their_messages(native):
+    # what FLK_ERR_DEVICE reports for each device error word (no GPU involved)
+    assert "scan look-back wait gave up" in native.device_error_text(1)
+    assert "outside its array" in native.device_error_text(2)
+    assert native.device_error_text(0) == "no device error"
+    assert native.device_error_text(77) == "unknown device error word"

@@ -16,6 +16,8 @@ Tolerances are written here, next to the checks.
 """
 from __future__ import annotations
 
+import re
+
 import numpy as np
 import pytest
 
@@ -392,15 +394,50 @@ def test_file_drop_in_and_cli(native, oracle, tmp_path):
     out = str(tmp_path / "end.flk")
     ref = str(tmp_path / "ref.flk")
     subprocess.run([oracle.CLI, "gen", "--birds", "2000", "--seed", "1", "--out", src], check=True)
-    r = subprocess.run([native.CLI_PATH, "--in", src, "--steps", "10", "--warmup", "2", "--out", out],
-                       capture_output=True, text=True)
+    r = subprocess.run([native.CLI_PATH, "--in", src, "--steps", "10", "--warmup", "2", "--out", out,
+                        "--decide-smem", "0"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    for name in ("grid_histogram", "grid_scan", "grid_scatter", "decide", "integrate", "step total",
-                 "bird-steps/s", "# 2000 birds, 10 steps (2 warm-up, not timed)"):
-        assert name in r.stdout
+    # stdout has the reference's layout line by line (cuda/flock.cu:399-401,440-445,486-491),
+    # apart from the program name
+    lines = r.stdout.splitlines()
+    header = [
+        r"# flock_gb300: .+ \(sm_\d+\), CUDA driver \d+\.\d+ runtime \d+\.\d+",
+        r"# 2000 birds, 10 steps \(2 warm-up, not timed\)",
+        r"# decide occupancy: \d+ blocks/SM of \d+ threads = \d+% of \d+ threads/SM \(dynamic smem \d+ B\)",
+        r"# 8 timed steps \(mean GPU ms per pass, CUDA events\)",
+    ] + [rf"  {name:<16} +\d+\.\d{{4}}" for name in ("grid_histogram", "grid_scan", "grid_scatter", "decide",
+                                                      "integrate", "step total")] + [r"  bird-steps/s +\d+"]
+    assert len(lines) == len(header), r.stdout
+    for line, pat in zip(lines, header):
+        assert re.fullmatch(pat, line), (line, pat)
+    # a reservation no decide CTA can hold is a usage error, as an unknown flag
+    big = subprocess.run([native.CLI_PATH, "--in", src, "--steps", "1", "--decide-smem", str(1 << 30)],
+                         capture_output=True, text=True)
+    assert big.returncode == 2 and "decide-smem" in big.stderr
     subprocess.run([oracle.CLI, "step", "--in", src, "--steps", "10", "--out", ref], check=True)
     d = subprocess.run([oracle.CLI, "diff", ref, out], capture_output=True, text=True)
     assert d.returncode == 0 and "neighbour-count mismatches 0 of 2000" in d.stdout, d.stdout
+
+
+def test_scan_wait_runs_out_and_returns_a_device_error(native, oracle):
+    # The scan's look-back waits are bounded. Here tile 0 of the next
+    # grid-reporting step publishes no flag (a flag nothing sets), every other
+    # tile's look-back gives up after 1000 polls, and the step reports
+    # FLK_ERR_DEVICE with the scan-timeout text instead of hanging.
+    w = native.generate(20_000, 1)  # buckets_for = 65,536: 16 scan tiles
+    f = native.Flock(w)
+    f.debug_scan_timeout(skip_tile=0, spin_limit=1000)
+    with pytest.raises(native.FlockError) as e:
+        f.step_debug()
+    assert e.value.code == -6 and "scan look-back wait gave up" in str(e.value)
+    f.close()
+    # the device and the process still answer: a fresh handle steps exactly
+    g = native.Flock(w)
+    dbg = g.step_debug()
+    g.close()
+    keys, offs, srt = oracle.grid(w, native.buckets_for(len(w)))
+    assert np.array_equal(dbg["keys"], keys) and np.array_equal(dbg["offsets"], offs)
+    assert np.array_equal(dbg["sorted"], srt)
 
 
 # ---- full-size sizes: size-independent properties -----------------------------
