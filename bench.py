@@ -560,7 +560,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--birds", type=int, default=1_000_000)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--no-extra", action="store_true", help="skip the batched / served / CPU measurements")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the batched / served / CPU / reference-kernel / other-size measurements")
     ap.add_argument("--batched-steps", type=int, default=30)
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=100.0)
@@ -616,12 +617,12 @@ def main():
     if rank == 0:
         out["e2e"] = bench_e2e(m, args, local)
         out["multi_step"] = bench_multi_step(m, args, local)
-        # the reference's own kernels on this GPU at the headline workload, with
-        # the reference's protocol for it (20 warm-up + 100 timed steps)
-        out["ref_gpu"] = ref_gpu(n, args.seed, 120, 20, local, words=m.generate(n, args.seed))
-        if "value" in out["ref_gpu"]:
-            out["ref_gpu"]["speedup"] = value / out["ref_gpu"]["value"]
         if not args.no_extra:
+            # the reference's own kernels on this GPU at the headline workload, with
+            # the reference's protocol for it (20 warm-up + 100 timed steps)
+            out["ref_gpu"] = ref_gpu(n, args.seed, 120, 20, local, words=m.generate(n, args.seed))
+            if "value" in out["ref_gpu"]:
+                out["ref_gpu"]["speedup"] = value / out["ref_gpu"]["value"]
             out["configs"] = bench_configs(m, local)
         if not args.no_extra:
             out["batched"] = bench_batched(m, args, local)

@@ -107,6 +107,8 @@ int flk_step_f64(flk_flock* f, double* out64, double* report);
  * the next step's grid. The first grid is counted before the first timed step
  * and one untimed step follows the last, so the flock advances steps + 1. */
 int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step);
+/* flk_batch_tune_cell for a plain flock. */
+int flk_tune_cell(flk_flock* f, float cell_m);
 /* Frees the flock's device memory (the cudaFree calls closing main,
  * cuda/flock.cu:520-523). */
 void flk_close(flk_flock* f);
@@ -143,6 +145,15 @@ int flk_batch_step_f64(flk_batch* b, const int32_t* ids, uint32_t count, double*
  * size, steps per captured graph. Zero keeps the current value. No
  * counterpart: the reference fixes its launch shapes (cuda/flock.cu:453-470). */
 int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t decide_threads, int32_t graph_chunk);
+/* Production cell edge in metres (default 4 m, the reference's; [2, 16],
+ * else FLK_ERR_ARG): the cells that steps without grid output sort birds
+ * into, in quarter-cell z-slabs, and search. It changes which candidates
+ * decide tests, never which neighbours it finds (exact distance tests decide
+ * membership); sums may change by rounding. Grid-reporting steps
+ * (flk_step_debug) always use the reference's 4 m cells
+ * (crates/flock-ref/src/params.rs:58, cuda/flock.cu:77-83). No counterpart:
+ * the reference's cell is a compile-time constant. */
+int flk_batch_tune_cell(flk_batch* b, float cell_m);
 /* Chunk graphs instantiated, and updated in place (cudaGraphExecUpdate, when
  * only sizes or pointers changed, e.g. a flock joined or left), so far. */
 int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated);

@@ -1,9 +1,14 @@
-"""Launch-shape autotuner for the flock engine.
+"""Launch-shape and cell-size autotuner for the flock engine.
 
 The engine's passes are persistent grid-stride kernels whose shapes are
 runtime parameters: CTAs per SM of the streaming passes (hash/count,
 scatter, integrate), `decide`'s CTA size and CTAs per SM, and the number of
-steps captured per CUDA graph. The best values depend on the workload (one
+steps captured per CUDA graph. The production steps' cell edge is one too
+(`cell`, in metres; cells are sorted in quarter-cell z-slabs): a smaller cell
+means fewer candidates per deciding bird but more cells per search box (a
+box of more than 32 cells leaves decide's fast path) and shorter runs for the
+sort. Any edge finds the same neighbours. Clusters are not used, so there is
+no cluster shape to tune. The best values depend on the workload (one
 1M-bird flock vs hundreds of small flocks), so the tuner measures them on the
 actual batch: coordinate descent over each knob's candidate values, each
 candidate timed with CUDA events over a few graph-launched steps, keeping a
@@ -22,12 +27,13 @@ import os
 from typing import Optional
 
 SPACE = {
+    "cell": [3.0, 3.5, 4.0, 5.0],
     "stream_bps": [4, 8, 16],
     "decide_bps": [1, 2, 4, 8],
     "decide_threads": [256, 512, 1024],
     "graph_chunk": [5, 10, 20],
 }
-DEFAULT = {"stream_bps": 8, "decide_bps": 1, "decide_threads": 1024, "graph_chunk": 10}
+DEFAULT = {"cell": 4.0, "stream_bps": 8, "decide_bps": 1, "decide_threads": 1024, "graph_chunk": 10}
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
@@ -44,7 +50,7 @@ def _signature(batch) -> str:
 
 def _apply(batch, shape: dict) -> None:
     batch.tune(stream_bps=shape["stream_bps"], decide_bps=shape["decide_bps"],
-               decide_threads=shape["decide_threads"], graph_chunk=shape["graph_chunk"])
+               decide_threads=shape["decide_threads"], graph_chunk=shape["graph_chunk"], cell=shape["cell"])
 
 
 def _time(batch, shape: dict, steps: int, reps: int) -> float:

@@ -65,6 +65,17 @@ __device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
 
 // cuda/flock.cu:77-83: cell = floor(p / 4), bucket = spatial hash & mask.
 __device__ __forceinline__ int cell1(float x) { return (int)floorf(__fmul_rn(x, INV_CELL)); }
+// Cell of coordinate x in a grid of edge 1 / inv_cell: floor(x * inv_cell),
+// monotonic in x for any edge; production steps use the same expression in
+// every pass (the edge is a runtime choice, the autotuner's `cell` axis).
+__device__ __forceinline__ int pcell(float x, float inv_cell) { return (int)floorf(__fmul_rn(x, inv_cell)); }
+// The quarter-cell z-slab of z within its cell cz (inv4 = 4 / edge), clamped
+// to 0..3 against the rounding of z * inv4 next to a cell boundary; decide's
+// slab trim stays conservative, since the slab index and floor(z * inv4)
+// move together.
+__device__ __forceinline__ uint32_t pslab(float z, int cz, float inv4) {
+    return (uint32_t)min(3, max(0, pcell(z, inv4) - 4 * cz));
+}
 __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz) {
     return ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ ((uint32_t)cz * 83492791u);
 }
@@ -99,18 +110,19 @@ struct SearchBox {
     long long nx, ny, nz, ncell;
     bool wide;
 };
-__device__ __forceinline__ SearchBox search_box(f3 p, float r) {
+// Cells of edge 1 / inv_cell (the reference's 4 m cells by default).
+__device__ __forceinline__ SearchBox search_box(f3 p, float r, float inv_cell = INV_CELL) {
     SearchBox b;
     const float rr = __fmul_rn(2.0f, r);
     const float pm = fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
     b.reach = rr * 1.00001f + 1e-3f + pm * 1e-6f;
     b.reach2 = b.reach * b.reach;
-    b.lx = cell1(p.x - b.reach);
-    b.ly = cell1(p.y - b.reach);
-    b.lz = cell1(p.z - b.reach);
-    b.nx = (long long)cell1(p.x + b.reach) - b.lx + 1;
-    b.ny = (long long)cell1(p.y + b.reach) - b.ly + 1;
-    b.nz = (long long)cell1(p.z + b.reach) - b.lz + 1;
+    b.lx = pcell(p.x - b.reach, inv_cell);
+    b.ly = pcell(p.y - b.reach, inv_cell);
+    b.lz = pcell(p.z - b.reach, inv_cell);
+    b.nx = (long long)pcell(p.x + b.reach, inv_cell) - b.lx + 1;
+    b.ny = (long long)pcell(p.y + b.reach, inv_cell) - b.ly + 1;
+    b.nz = (long long)pcell(p.z + b.reach, inv_cell) - b.lz + 1;
     b.wide = b.nx > (1 << 20) || b.ny > (1 << 20) || b.nz > (1 << 20);
     b.ncell = b.wide ? (1ll << 62) : b.nx * b.ny * b.nz;
     return b;

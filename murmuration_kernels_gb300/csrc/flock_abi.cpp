@@ -411,6 +411,23 @@ extern "C" int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_b
     });
 }
 
+static int set_cell(Engine& e, float cell_m) {
+    flk::LaunchShape s = e.shape();
+    s.cell = cell_m;
+    e.set_shape(s);  // rejects an edge outside [2, 16] m
+    return FLK_OK;
+}
+
+extern "C" int flk_batch_tune_cell(flk_batch* b, float cell_m) {
+    if (!b) return fail(FLK_ERR_ARG, "flk_batch_tune_cell: null handle");
+    return guarded([&] { return set_cell(*b->eng, cell_m); });
+}
+
+extern "C" int flk_tune_cell(flk_flock* f, float cell_m) {
+    if (!f) return fail(FLK_ERR_ARG, "flk_tune_cell: null handle");
+    return guarded([&] { return set_cell(*f->eng, cell_m); });
+}
+
 extern "C" int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated) {
     if (!b || !instantiated || !updated) return fail(FLK_ERR_ARG, "flk_batch_graph_counts: null pointer");
     b->eng->graph_counts(instantiated, updated);

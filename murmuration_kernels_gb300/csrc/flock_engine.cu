@@ -175,6 +175,7 @@ void Engine::set_shape(const LaunchShape& s) {
     if (need > (size_t)optin)
         throw Error{-1, "decide would need " + std::to_string(need) + " B of shared memory per CTA, above the " +
                             std::to_string(optin) + " B a CTA may have"};
+    if (!(s.cell >= 2.0f && s.cell <= 16.0f)) throw Error{-1, "production cell edge must lie in [2, 16] m"};
     shape_ = s;
     // decide's dynamic shared memory grows with its CTA size; allow past 48 KB
     FLK_CUDA(cudaFuncSetAttribute(k_decide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -662,9 +663,11 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
     auto sgrid = [&](int f) { return pgrid(num_sms_, std::min(shape_.stream_blocks_per_sm, f), V_, 256); };
     const uint32_t ntiles = Btot_ / SCAN_TILE;
     const GridBuf g = grid_buf(buf), gn = grid_buf(buf ^ 1);
+    const float cell = shape_.cell, inv_cell = 1.0f / shape_.cell;  // production cells
     if (ev) FLK_CUDA(cudaEventRecord(ev[0], stream_));
     if (sets)  // a grid-reporting step: the reference's cell hash
-        k_hash_count<false><<<sgrid(fit_.hash[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_);
+        k_hash_count<false><<<sgrid(fit_.hash[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, key_, arrival_, g, ctl_,
+                                                                      INV_CELL);
     else if (hash)
         enqueue_hash(buf);
     if (ev) FLK_CUDA(cudaEventRecord(ev[1], stream_));
@@ -682,7 +685,7 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
         table_d_, nfl, V_, ctl_, g.occ, offsets_, g.counts, g.occ_count, tmp_, ar_, sfwd_, due_, slabs_);
     if (f64) {  // FP64 evaluation from the input state, before the f32 passes change it
         k_decide_f64<<<pgrid(num_sms_, fit_.decide_f64, V_, 8), 256, 0, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
-                                                                      g.counts, ar_, dec64_, err64_);
+                                                                      g.counts, ar_, dec64_, err64_, cell, inv_cell);
         k_integrate_f64<<<sgrid(fit_.integrate_f64), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, dec64_, out64_);
     }
     if (ev) FLK_CUDA(cudaEventRecord(ev[3], stream_));
@@ -692,16 +695,18 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
     if (sets)
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                        g.counts, ar_, sfwd_, radius_table_, sets_,
-                                                                       slabs_);
+                                                                       slabs_, GRID_CELL, INV_CELL);
     else
         k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                         g.counts, ar_, sfwd_, radius_table_, nullptr,
-                                                                        slabs_);
+                                                                        slabs_, cell, inv_cell);
     if (ev) FLK_CUDA(cudaEventRecord(ev[4], stream_));
     if (fuse_next && !sets)
-        k_integrate<true><<<sgrid(fit_.integrate[1]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
+        k_integrate<true><<<sgrid(fit_.integrate[1]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_,
+                                                                         inv_cell);
     else
-        k_integrate<false><<<sgrid(fit_.integrate[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_);
+        k_integrate<false><<<sgrid(fit_.integrate[0]), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, g, gn, key_, arrival_, ctl_,
+                                                                          inv_cell);
     if (f64) k_compare_f64<<<sgrid(fit_.compare_f64), 256, 0, stream_>>>(table_d_, nfl, V_, ar_, active_, out64_, err64_);
     if (ev) FLK_CUDA(cudaEventRecord(ev[5], stream_));
 }
@@ -710,7 +715,7 @@ void Engine::enqueue_hash(int buf) {
     device_ahead_ = true;
     const int grid = pgrid(num_sms_, std::min(shape_.stream_blocks_per_sm, fit_.hash[1]), V_, 256);
     k_hash_count<true><<<grid, 256, 0, stream_>>>(table_d_, (int)table_h_.size(), V_, ar_, key_, arrival_,
-                                                  grid_buf(buf), ctl_);
+                                                  grid_buf(buf), ctl_, 1.0f / shape_.cell);
 }
 
 void Engine::enqueue_steps(uint32_t n) {

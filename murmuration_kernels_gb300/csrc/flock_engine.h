@@ -105,6 +105,7 @@ struct LaunchShape {
     int segsort_blocks_per_sm = 8;  // segment-sort CTAs per SM (256 threads)
     int graph_chunk = 10;           // steps per captured CUDA graph
     size_t decide_extra_smem = 0;   // dynamic shared memory reserved beyond decide's own (occupancy experiments)
+    float cell = 4.0f;              // production cell edge (m); any edge gives the same neighbour sets
 };
 
 struct GridDebug {  // host copies of one step's grid and neighbour-set summaries

@@ -167,13 +167,15 @@ __device__ __forceinline__ void enqueue2(Sweep& w, bool hA, uint32_t tA, bool hB
     }
 }
 
-// Cheap-phase test of candidate t; CHECK_CELL also requires cell (cx,cy,cz).
+// Cheap-phase test of candidate t; CHECK_CELL also requires cell (cx,cy,cz) of
+// edge 1 / inv_cell.
 template <bool CHECK_CELL>
-__device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int cy, int cz) {
+__device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int cy, int cz, float inv_cell) {
     const float dx = __fsub_rn(q.x, w.p.x), dy = __fsub_rn(q.y, w.p.y), dz = __fsub_rn(q.z, w.p.z);
     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     bool hit = d2 <= w.c2;
-    if (CHECK_CELL) hit = hit && cell1(q.x) == cx && cell1(q.y) == cy && cell1(q.z) == cz;
+    if (CHECK_CELL)
+        hit = hit && pcell(q.x, inv_cell) == cx && pcell(q.y, inv_cell) == cy && pcell(q.z, inv_cell) == cz;
     return hit;
 }
 
@@ -184,18 +186,18 @@ __device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int
 // measured to round d2 differently, admitting a bird one ulp outside 2R
 // (test_two_birds_one_ulp_outside_2r), and cost no time to give up.
 __device__ __forceinline__ void near2(const Sweep& w, const float4 qa, const float4 qb, bool& ha, bool& hb) {
-    ha = near<false>(w, qa, 0, 0, 0);
-    hb = near<false>(w, qb, 0, 0, 0);
+    ha = near<false>(w, qa, 0, 0, 0, 0.f);
+    hb = near<false>(w, qb, 0, 0, 0, 0.f);
 }
 
 // Cheap phase over one contiguous candidate range [sc, ec) (wide paths).
 template <bool SETS, bool CHECK_CELL>
 __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32_t lane, int cx = 0, int cy = 0,
-                                      int cz = 0) {
+                                      int cz = 0, float inv_cell = 0.f) {
     for (uint32_t base = sc; base < ec; base += 32) {
         const uint32_t t = base + lane;
         bool hit = false;
-        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.pos[t + w.shift]), cx, cy, cz);
+        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.pos[t + w.shift]), cx, cy, cz, inv_cell);
         enqueue<SETS>(w, hit, t, lane);
     }
 }
@@ -317,6 +319,7 @@ struct WarpSmem {
     static constexpr int NI = SETS ? 8 : 4;  // integer sums per bird
     int4 box[32];          // the next 32 birds' search boxes (group_boxes)
     uint4 aux[32];
+    int2 zc[32];           // their first cell along z and cell count along z
     uint32_t queue[96];
     float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
     uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
@@ -327,27 +330,32 @@ struct WarpSmem {
 
 // Search boxes of a warp's next 32 deciding birds (records e, e + nw, ...,
 // e + 31 nw), one bird per lane, so the box arithmetic runs once per bird
-// rather than once per lane of a warp-uniform setup. box: first cell x, y;
-// floor(z - reach), floor(z + reach). aux: reach^2 (f32 bits); mx | nx << 17;
-// my | ny << 17 (multiply-shift constants, div_magic); the lattice bit counts
-// (lattice_bits) | 1 << 31 when the box has at most 32 cells (the fast path).
+// rather than once per lane of a warp-uniform setup. Cells of edge
+// 1 / inv_cell (the reference's 4 m cells in SETS steps). box: first cell x,
+// y; the z-slab range floor((z -/+ reach) * 4 inv_cell) (slabs of a quarter
+// cell). aux: reach^2 (f32 bits); mx | nx << 17; my | ny << 17 (multiply-shift
+// constants, div_magic); the lattice bit counts (lattice_bits) | 1 << 31 when
+// the box has at most 32 cells (the fast path). zc: first cell along z, cells
+// along z.
 template <bool SETS>
 __device__ __forceinline__ void group_boxes(WarpSmem<SETS>& m, const DueRec* __restrict__ due, uint32_t e,
-                                            uint32_t nw, uint32_t ndue, uint32_t lane) {
+                                            uint32_t nw, uint32_t ndue, uint32_t lane, float inv_cell) {
     const uint32_t ej = e + lane * nw;
     if (ej < ndue) {
         const float4 pr = due[ej].pr;
         const uint32_t buckets = due[ej].fl.z;
-        const SearchBox sb = search_box(mk(pr.x, pr.y, pr.z), pr.w);
+        const SearchBox sb = search_box(mk(pr.x, pr.y, pr.z), pr.w, inv_cell);
         int4 box = make_int4(sb.lx, sb.ly, 0, 0);
         uint4 aux = make_uint4(__float_as_uint(sb.reach2), 0u, 0u, 0u);
         if (sb.ncell <= 32) {
             const uint32_t nx = (uint32_t)sb.nx, ny = (uint32_t)sb.ny;
-            box.z = (int)floorf(pr.z - sb.reach);
-            box.w = (int)floorf(pr.z + sb.reach);
+            const float inv4 = __fmul_rn(4.0f, inv_cell);
+            box.z = pcell(pr.z - sb.reach, inv4);
+            box.w = pcell(pr.z + sb.reach, inv4);
             aux.y = div_magic(nx) | (nx << 17);
             aux.z = div_magic(ny) | (ny << 17);
             aux.w = lattice_bits(buckets) | (1u << 31);
+            m.zc[lane] = make_int2(sb.lz, (int)sb.nz);
         }
         m.box[lane] = box;
         m.aux[lane] = aux;
@@ -414,7 +422,8 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                                                                       const float4* __restrict__ sfwd,
                                                                       const float* __restrict__ rtab,
                                                                       uint32_t* __restrict__ sets,
-                                                                      const uint32_t* __restrict__ slabs) {
+                                                                      const uint32_t* __restrict__ slabs,
+                                                                      float pcell_edge, float pinv_cell) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     WarpSmem<SETS>& m = reinterpret_cast<WarpSmem<SETS>*>(s_raw)[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
@@ -423,6 +432,8 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
     const uint32_t ndue = *(volatile uint32_t*)&ctl->due_count;
     uint32_t cand = 0, pairs = 0, slot = 0;
 
+    // SETS steps: the reference's 4 m cells; production steps: the runtime edge
+    const float cell = SETS ? GRID_CELL : pcell_edge, inv_cell = SETS ? INV_CELL : pinv_cell;
     Sweep w;
     w.pos = ar.A;
     w.bid = ar.id;
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
     w.qn = 0;
 
     for (uint32_t e = gw; e < ndue; e += nw) {
-        if (slot == 0) group_boxes<SETS>(m, due, e, nw, ndue, lane);
+        if (slot == 0) group_boxes<SETS>(m, due, e, nw, ndue, lane, inv_cell);
         const int4 box = m.box[slot];
         const uint4 aux = m.aux[slot];
         const DueRec rec = due[e];  // everything the setup needs, one place
@@ -457,8 +468,9 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             const float reach2 = __uint_as_float(aux.x);
             const uint32_t nx = aux.y >> 17, ny = aux.z >> 17;
             const int lx = box.x, ly = box.y, zlo = box.z, zhi = box.w;
-            const int lz = zlo >> 2;  // floor(floor(z - reach) / 4) = floor((z - reach) / 4)
-            const uint32_t ncell = nx * ny * (uint32_t)((zhi >> 2) - lz + 1);
+            const int2 zc = m.zc[slot];
+            const int lz = zc.x;
+            const uint32_t ncell = nx * ny * (uint32_t)zc.y;
             bool valid = false;
             uint32_t b = 0;
             int z0 = 0, z1 = 3;  // production steps: the z-slabs of this lane's cell within reach
@@ -472,10 +484,10 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                     z0 = min(3, max(0, zlo - 4 * cz));
                     z1 = min(3, max(0, zhi - 4 * cz));
                 }
-                const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
-                const float dx = fminf(fmaxf(p.x, ox), ox + GRID_CELL) - p.x;
-                const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
-                const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
+                const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
+                const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
+                const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
+                const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
                 valid = dx * dx + dy * dy + dz * dz <= reach2;
                 b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
                                   : lattice_bucket_bits(cx, cy, cz, aux.w));
@@ -488,11 +500,11 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             }
             uint32_t s = 0, en = 0;
             if (keep) {
-                // Production runs are ordered by 1 m z-slab within their cell, and
-                // the sort left each run's slab boundaries (birds in slabs < 1, < 2,
-                // < 3; 10 bits each; all ones: untrimmed). A candidate within the
-                // reach has |dz| <= reach and floor is monotonic, so only slabs
-                // z0..z1 of this cell can hold one: the range shrinks to them.
+                // Production runs are ordered by quarter-cell z-slab within their
+                // cell, and the sort left each run's slab boundaries (birds in slabs
+                // < 1, < 2, < 3; 10 bits each; all ones: untrimmed). A candidate
+                // within the reach has |dz| <= reach and floor is monotonic, so only
+                // slabs z0..z1 of this cell can hold one: the range shrinks to them.
                 // (The trim takes the bucket's cell to be this lane's: no two cells of
                 // the box share a bucket in production steps, since the box spans at
                 // most 3 cells per axis and the lattice index repeats only every 16
@@ -516,7 +528,7 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
             cand += en - s;
             sweep_packed<SETS>(w, s, en, lane);
         } else {
-            const SearchBox sb = search_box(p, r);
+            const SearchBox sb = search_box(p, r, inv_cell);
             const float reach2 = sb.reach2;
             const int lx = sb.lx, ly = sb.ly, lz = sb.lz;
             const long long nxl = sb.nx, nyl = sb.ny, ncell = sb.ncell;
@@ -541,10 +553,10 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                         const long long t = ci / nxl;
                         cy = ly + (int)(t % nyl);
                         cz = lz + (int)(t / nyl);
-                        const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
-                        const float dx = fminf(fmaxf(p.x, ox), ox + GRID_CELL) - p.x;
-                        const float dy = fminf(fmaxf(p.y, oy), oy + GRID_CELL) - p.y;
-                        const float dz = fminf(fmaxf(p.z, oz), oz + GRID_CELL) - p.z;
+                        const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
+                        const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
+                        const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
+                        const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
                         valid = dx * dx + dy * dy + dz * dz <= reach2;
                         if (valid) {
                             bucket_range(offsets, counts, bbase + bucket_of<SETS>(cx, cy, cz, buckets), V, w.shift,
@@ -560,7 +572,7 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
                         const uint32_t sc = __shfl_sync(FULL, s, c), ec = __shfl_sync(FULL, en, c);
                         const int ccx = __shfl_sync(FULL, cx, c), ccy = __shfl_sync(FULL, cy, c),
                                   ccz = __shfl_sync(FULL, cz, c);
-                        sweep<SETS, true>(w, sc, ec, lane, ccx, ccy, ccz);
+                        sweep<SETS, true>(w, sc, ec, lane, ccx, ccy, ccz, inv_cell);
                     }
                 }
             }

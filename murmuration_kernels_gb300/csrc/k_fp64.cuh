@@ -69,16 +69,18 @@ __device__ __forceinline__ double wsum(double v) {
     return v;
 }
 
-// One warp per deciding bird. Candidates: every distinct bucket of the cells a
-// conservative 2r box touches (the f32 step's reach bounds every FP64 pair as
-// well), or the flock's whole range when the box is wide. dec[view] receives
+// One warp per deciding bird. Candidates: every distinct bucket of the
+// production cells (edge `cell`) a conservative 2r box touches (the f32
+// step's reach bounds every FP64 pair as well), or the flock's whole range
+// when the box is wide. dec[view] receives
 // steering xyz, radius, neighbour count, centrality, next decision; err[4f + 3]
 // counts flock f's deciding birds.
 __global__ void __launch_bounds__(256) k_decide_f64(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                     StepCtl* __restrict__ ctl, const DueRec* __restrict__ due,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ counts, Arena ar,
-                                                    double* __restrict__ dec, uint32_t* __restrict__ err) {
+                                                    double* __restrict__ dec, uint32_t* __restrict__ err, float cell,
+                                                    float inv_cell) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -96,10 +98,11 @@ __global__ void __launch_bounds__(256) k_decide_f64(const FlockDesc* __restrict_
         const float pm = fmaxf(fabsf(a_me.x), fmaxf(fabsf(a_me.y), fabsf(a_me.z)));
         const float reach = rr * 1.00001f + 1e-3f + pm * 1e-6f;
         const float reach2 = reach * reach;
-        const int lx = cell1(a_me.x - reach), ly = cell1(a_me.y - reach), lz = cell1(a_me.z - reach);
-        const long long nxl = (long long)cell1(a_me.x + reach) - lx + 1,
-                        nyl = (long long)cell1(a_me.y + reach) - ly + 1,
-                        nzl = (long long)cell1(a_me.z + reach) - lz + 1;
+        const int lx = pcell(a_me.x - reach, inv_cell), ly = pcell(a_me.y - reach, inv_cell),
+                  lz = pcell(a_me.z - reach, inv_cell);
+        const long long nxl = (long long)pcell(a_me.x + reach, inv_cell) - lx + 1,
+                        nyl = (long long)pcell(a_me.y + reach, inv_cell) - ly + 1,
+                        nzl = (long long)pcell(a_me.z + reach, inv_cell) - lz + 1;
         const bool wide = nxl > (1 << 20) || nyl > (1 << 20) || nzl > (1 << 20);
         const long long ncell = wide ? (1ll << 62) : nxl * nyl * nzl;
         Acc64 acc;
@@ -113,10 +116,10 @@ __global__ void __launch_bounds__(256) k_decide_f64(const FlockDesc* __restrict_
                 const int cx = lx + (int)lane % nx;
                 const int t = (int)lane / nx;
                 const int cy = ly + t % ny, cz = lz + t / ny;
-                const float ox = (float)cx * GRID_CELL, oy = (float)cy * GRID_CELL, oz = (float)cz * GRID_CELL;
-                const float dx = fminf(fmaxf(a_me.x, ox), ox + GRID_CELL) - a_me.x;
-                const float dy = fminf(fmaxf(a_me.y, oy), oy + GRID_CELL) - a_me.y;
-                const float dz = fminf(fmaxf(a_me.z, oz), oz + GRID_CELL) - a_me.z;
+                const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
+                const float dx = fminf(fmaxf(a_me.x, ox), ox + cell) - a_me.x;
+                const float dy = fminf(fmaxf(a_me.y, oy), oy + cell) - a_me.y;
+                const float dz = fminf(fmaxf(a_me.z, oz), oz + cell) - a_me.z;
                 valid = dx * dx + dy * dy + dz * dz <= reach2;
                 b = bbase + lattice_bucket(cx, cy, cz, buckets);
             }

@@ -103,15 +103,20 @@ __device__ __forceinline__ void count_block(bool act, uint32_t v, uint32_t b, ui
     if (first) g.occ[s_first[it][warp] + __popc(fm & lanemask_lt())] = b;
 }
 
-// Cell of position p as its bucket (LATTICE: lattice_bucket; otherwise the
-// reference's cell hash, whose keys a grid-reporting step returns) and, in
-// production steps, its 1 m z-slab within the cell.
+// Cell of position p as its bucket (LATTICE: lattice_bucket of the
+// production cell of edge 1 / inv_cell; otherwise the reference's 4 m cell
+// and hash, whose keys a grid-reporting step returns) and, in production
+// steps, its quarter-cell z-slab within the cell (inv4 = 4 * inv_cell).
 template <bool LATTICE>
-__device__ __forceinline__ uint32_t bucket_slab(const float4 p, uint32_t bbase, uint32_t nb, uint32_t& slab) {
-    const int cx = cell1(p.x), cy = cell1(p.y), cz = cell1(p.z);
-    // floor(z) - 4 * floor(z / 4): z * 0.25 is exact, so this agrees with cell1
-    slab = LATTICE ? ((uint32_t)((int)floorf(p.z) - 4 * cz) & 3u) : 0u;
-    return bbase + (LATTICE ? lattice_bucket(cx, cy, cz, nb) : (cell_hash(cx, cy, cz) & (nb - 1u)));
+__device__ __forceinline__ uint32_t bucket_slab(const float4 p, uint32_t bbase, uint32_t nb, uint32_t& slab,
+                                                float inv_cell, float inv4) {
+    if (!LATTICE) {
+        slab = 0u;
+        return bbase + (cell_hash(cell1(p.x), cell1(p.y), cell1(p.z)) & (nb - 1u));
+    }
+    const int cx = pcell(p.x, inv_cell), cy = pcell(p.y, inv_cell), cz = pcell(p.z, inv_cell);
+    slab = pslab(p.z, cz, inv4);
+    return bbase + lattice_bucket(cx, cy, cz, nb);
 }
 
 // LATTICE: a production step, whose sort orders each run by z-slab (the slab
@@ -121,7 +126,7 @@ template <bool LATTICE>
 __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
                                                     Arena ar, uint32_t* __restrict__ key,
                                                     uint32_t* __restrict__ arrival, GridBuf g,
-                                                    StepCtl* __restrict__ ctl) {
+                                                    StepCtl* __restrict__ ctl, float inv_cell) {
     __shared__ uint32_t s_first[2][8];  // per warp: first-seen buckets, then their start in occ
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t it = 0;
@@ -133,7 +138,8 @@ __global__ void __launch_bounds__(256) k_hash_count(const FlockDesc* __restrict_
             const FlockDesc* d = &fl[find_flock_v(fl, nfl, v)];
             if (__ldg(&d->remaining)) {
                 const float4 p = ar.A[v + view_shift(__ldg(&d->sbase), __ldg(&d->vbase), __ldg(&d->parity), ar.cap)];
-                b = bucket_slab<LATTICE>(p, __ldg(&d->bbase), __ldg(&d->buckets), slab);
+                b = bucket_slab<LATTICE>(p, __ldg(&d->bbase), __ldg(&d->buckets), slab, inv_cell,
+                                         __fmul_rn(4.0f, inv_cell));
                 key[v] = b;
                 act = true;
             }

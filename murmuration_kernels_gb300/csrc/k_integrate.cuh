@@ -15,11 +15,13 @@ namespace flk {
 // FUSE (production runs of several steps): also counts the next step's grid
 // from the new positions into grid buffer nxt (key, arrival rank, histogram)
 // for every flock that steps again, so the next step needs no separate hash
-// pass; the counting is count_block, as in k_hash_count<true>.
+// pass; the counting is count_block, as in k_hash_count<true> (production
+// cells of edge 1 / inv_cell).
 template <bool FUSE>
 __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, int nfl, uint32_t V, Arena ar,
                                                    GridBuf cur, GridBuf nxt, uint32_t* __restrict__ key,
-                                                   uint32_t* __restrict__ arrival, StepCtl* __restrict__ ctl) {
+                                                   uint32_t* __restrict__ arrival, StepCtl* __restrict__ ctl,
+                                                   float inv_cell) {
     __shared__ uint32_t s_first[2][8];
     // the histogram's occupied entries go back to zero for the step after next
     const uint32_t nocc = *(volatile const uint32_t*)cur.occ_count;
@@ -80,7 +82,8 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
                 A[st] = make_float4(pos.x, pos.y, pos.z, beta);
                 B[st] = make_float4(vel.x, vel.y, vel.z, rate);
                 if (FUSE && rem >= 2) {  // this flock steps again: its bird's cell for the next step
-                    b = bucket_slab<true>(make_float4(pos.x, pos.y, pos.z, 0.f), d->bbase, d->buckets, slab);
+                    b = bucket_slab<true>(make_float4(pos.x, pos.y, pos.z, 0.f), d->bbase, d->buckets, slab,
+                                          inv_cell, __fmul_rn(4.0f, inv_cell));
                     key[v] = b;
                     act = true;
                 }

@@ -29,9 +29,9 @@ class FakeBatch:
         self.shape = None
         self.applied = []
 
-    def tune(self, stream_bps, decide_bps, decide_threads, graph_chunk):
+    def tune(self, stream_bps, decide_bps, decide_threads, graph_chunk, cell):
         self.shape = dict(stream_bps=stream_bps, decide_bps=decide_bps, decide_threads=decide_threads,
-                          graph_chunk=graph_chunk)
+                          graph_chunk=graph_chunk, cell=cell)
         self.applied.append(dict(self.shape))
 
     def time_steps(self, k):
@@ -41,7 +41,7 @@ class FakeBatch:
 def test_descent_finds_the_fastest_shape_one_knob_at_a_time(tmp_path, monkeypatch):
     at = _autotune()
     monkeypatch.setattr(at, "CACHE", str(tmp_path / "autotune.json"))
-    best = {"stream_bps": 16, "decide_bps": 2, "decide_threads": 512, "graph_chunk": 20}
+    best = {"stream_bps": 16, "decide_bps": 2, "decide_threads": 512, "graph_chunk": 20, "cell": 3.5}
     # separable cost: each knob away from its best value adds time
     cost = lambda s: 1.0 + sum(0.1 * (s[k] != best[k]) for k in best)
     b = FakeBatch(cost)
@@ -65,7 +65,7 @@ def test_changes_within_the_noise_margin_are_not_taken(tmp_path, monkeypatch):
 def test_cache_round_trip_and_signature(tmp_path, monkeypatch):
     at = _autotune()
     monkeypatch.setattr(at, "CACHE", str(tmp_path / "autotune.json"))
-    best = {"stream_bps": 4, "decide_bps": 1, "decide_threads": 1024, "graph_chunk": 5}
+    best = {"stream_bps": 4, "decide_bps": 1, "decide_threads": 1024, "graph_chunk": 5, "cell": 4.0}
     cost = lambda s: 1.0 + sum(0.1 * (s[k] != best[k]) for k in best)
     b = FakeBatch(cost)
     r1 = at.tune(b, steps=10)
@@ -78,3 +78,15 @@ def test_cache_round_trip_and_signature(tmp_path, monkeypatch):
     # another size profile (other decades) is a different signature
     b3 = FakeBatch(cost, sizes=(5, 50))
     assert at.cached(b3) is None
+
+
+def test_cell_axis_is_searched_first_and_kept_only_when_faster(tmp_path, monkeypatch):
+    at = _autotune()
+    monkeypatch.setattr(at, "CACHE", str(tmp_path / "autotune.json"))
+    assert list(at.SPACE)[0] == "cell" and at.DEFAULT["cell"] == 4.0
+    # a 5 m cell is 3 % faster for this mix; every other knob is neutral
+    cost = lambda s: 0.97 if s["cell"] == 5.0 else 1.0
+    b = FakeBatch(cost)
+    r = at.tune(b, steps=10, use_cache=False)
+    assert r["shape"]["cell"] == 5.0 and b.shape["cell"] == 5.0
+    assert {k: v for k, v in r["shape"].items() if k != "cell"} == {k: v for k, v in at.DEFAULT.items() if k != "cell"}

@@ -275,6 +275,43 @@ def test_dense_cell_and_long_ranges(native, oracle, per_cell):
     assert_step_parity(native, oracle, np.concatenate([w, extra]))
 
 
+def test_dense_production_cell_and_long_runs(native, oracle):
+    # 2000 birds in one 3 m cube: production buckets of more than 128 birds
+    # (ranked by counting) next to a flock of ordinary runs
+    rng = np.random.default_rng(17)
+    pos = rng.uniform(0.0, 3.0, size=(2000, 3)) + np.array([10.0, -6.0, 96.0])
+    w = np.stack([bird(p, radius=0.3, next_decision=rng.uniform(0, 0.01)) for p in pos]).astype(np.float32)
+    assert_step_parity(native, oracle, np.concatenate([w, oracle.scatter(3000, 17)]))
+
+
+@pytest.mark.parametrize("cell", [2.5, 3.0, 4.0, 5.0])
+def test_production_cell_edges_decide_the_same(native, oracle, cell):
+    # the production cell edge changes which candidates decide tests, never the
+    # neighbours it finds: every edge the autotuner may pick (3, 3.5, 4, 5 m
+    # among them) and one whose boxes mostly take the cell walk (2.5 m), from
+    # the same state
+    w = native.generate(100_000, 1)
+    t_cpu, c, _, _ = oracle.step(w, 0.0)
+    f = native.Flock(w)
+    f.tune_cell(cell)
+    f.step(1)
+    tp, gp = f.read()
+    f.close()
+    assert tp == t_cpu
+    assert_state_parity(gp, c, oracle)
+    # wide radii take the production cell walk and brute force at this edge too
+    v = oracle.scatter(4000, 11)
+    v[:200, 8] = 5.0
+    v[200:210, 8] = 60.0
+    v[:, 12] = 0.0
+    _, cv, _, _ = oracle.step(v, 0.0)
+    g = native.Flock(v)
+    g.tune_cell(cell)
+    g.step(1)
+    assert_state_parity(g.read()[1], cv, oracle)
+    g.close()
+
+
 def test_wide_radii_take_the_cell_walk_and_brute_force_paths(native, oracle):
     w = oracle.scatter(4000, 11)
     w[:200, 8] = 5.0    # 2R = 10 m: > 32 cells, cell walk with the exact cell check
