@@ -303,6 +303,8 @@ def bench_plain(m, args, dist, local):
     n, K, W = args.birds, args.steps, max(3, args.warmup)
     words = m.generate(n, args.seed)
     f = m.Flock(words, 0.0, device=local)
+    if args.decide == "staged":
+        f.tune_decide(1)
     f.step(W)
     barrier(dist)
     with ClockSampler(local) as clk:
@@ -567,6 +569,8 @@ def main():
     ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--chunk", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--decide", choices=["direct", "staged"], default="direct",
+                    help="the headline step's decide kernel (staged: neighbourhoods in shared memory)")
     args = ap.parse_args()
 
     dist, rank, world, local = dist_setup()

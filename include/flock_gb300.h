@@ -109,6 +109,8 @@ int flk_step_f64(flk_flock* f, double* out64, double* report);
 int flk_time_steps(flk_flock* f, uint32_t steps, uint64_t flush_bytes, float* ms_per_step);
 /* flk_batch_tune_cell for a plain flock. */
 int flk_tune_cell(flk_flock* f, float cell_m);
+/* flk_batch_tune_decide for a plain flock. */
+int flk_tune_decide(flk_flock* f, int32_t staged);
 /* Frees the flock's device memory (the cudaFree calls closing main,
  * cuda/flock.cu:520-523). */
 void flk_close(flk_flock* f);
@@ -154,6 +156,14 @@ int flk_batch_tune(flk_batch* b, int32_t stream_bps, int32_t decide_bps, int32_t
  * (crates/flock-ref/src/params.rs:58, cuda/flock.cu:77-83). No counterpart:
  * the reference's cell is a compile-time constant. */
 int flk_batch_tune_cell(flk_batch* b, float cell_m);
+/* Which decide kernel steps without grid output run (0, the default, sweeps
+ * the cell-ordered state through the caches; 1 stages each CTA's
+ * neighbourhood in shared memory with TMA bulk copies first, falling back to
+ * the direct sweep where birds of several flocks meet). Both find the same
+ * neighbours and give the same decisions; sums may differ by rounding. Other
+ * values: FLK_ERR_ARG. No counterpart: the reference's decide
+ * (cuda/flock.cu:190-290) reads every candidate from global memory. */
+int flk_batch_tune_decide(flk_batch* b, int32_t staged);
 /* Chunk graphs instantiated, and updated in place (cudaGraphExecUpdate, when
  * only sizes or pointers changed, e.g. a flock joined or left), so far. */
 int flk_batch_graph_counts(flk_batch* b, uint64_t* instantiated, uint64_t* updated);

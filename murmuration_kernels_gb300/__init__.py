@@ -93,6 +93,8 @@ _SIGS = {
     "flk_batch_tune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "flk_batch_tune_cell": (C.c_int, [_P, C.c_float]),
     "flk_tune_cell": (C.c_int, [_P, C.c_float]),
+    "flk_batch_tune_decide": (C.c_int, [_P, C.c_int32]),
+    "flk_tune_decide": (C.c_int, [_P, C.c_int32]),
     "flk_batch_counters": (C.c_int, [_P, _PU64, _PU64, _PU64]),
     "flk_batch_time_steps": (C.c_int, [_P, C.c_uint32, _PD]),
     "flk_batch_step_timed": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(PassTimes)]),
@@ -318,6 +320,10 @@ class Flock:
         """The production cell edge in m (steps without grid output)."""
         _check(lib().flk_tune_cell(self._h, C.c_float(cell)))
 
+    def tune_decide(self, staged: int) -> None:
+        """The production decide kernel: 0 sweeps the state, 1 stages cells in shared memory."""
+        _check(lib().flk_tune_decide(self._h, staged))
+
     def debug_scan_timeout(self, skip_tile: int = 0, spin_limit: int = 1000) -> None:
         """Test hook: the next step_debug's scan gives up waiting (FLK_ERR_DEVICE)."""
         _check(lib().flk_debug_scan_timeout(self._h, skip_tile, spin_limit))
@@ -427,11 +433,14 @@ class Batch:
         return a.value, b.value
 
     def tune(self, stream_bps: int = 0, decide_bps: int = 0, decide_threads: int = 0, graph_chunk: int = 0,
-             cell: float = 0.0) -> None:
-        """Launch shapes and the production cell edge in m (0 keeps a value)."""
+             cell: float = 0.0, staged: int = -1) -> None:
+        """Launch shapes, the production cell edge in m (0 keeps a value) and
+        the decide kernel (0 direct, 1 staged; -1 keeps it)."""
         _check(lib().flk_batch_tune(self._h, stream_bps, decide_bps, decide_threads, graph_chunk))
         if cell:
             _check(lib().flk_batch_tune_cell(self._h, C.c_float(cell)))
+        if staged >= 0:
+            _check(lib().flk_batch_tune_decide(self._h, staged))
 
     def time_steps(self, steps: int) -> float:
         ms = C.c_double()

@@ -418,6 +418,23 @@ static int set_cell(Engine& e, float cell_m) {
     return FLK_OK;
 }
 
+static int set_decide(Engine& e, int32_t staged) {
+    flk::LaunchShape s = e.shape();
+    s.decide_kind = staged;
+    e.set_shape(s);  // rejects anything but 0 or 1
+    return FLK_OK;
+}
+
+extern "C" int flk_batch_tune_decide(flk_batch* b, int32_t staged) {
+    if (!b) return fail(FLK_ERR_ARG, "flk_batch_tune_decide: null handle");
+    return guarded([&] { return set_decide(*b->eng, staged); });
+}
+
+extern "C" int flk_tune_decide(flk_flock* f, int32_t staged) {
+    if (!f) return fail(FLK_ERR_ARG, "flk_tune_decide: null handle");
+    return guarded([&] { return set_decide(*f->eng, staged); });
+}
+
 extern "C" int flk_batch_tune_cell(flk_batch* b, float cell_m) {
     if (!b) return fail(FLK_ERR_ARG, "flk_batch_tune_cell: null handle");
     return guarded([&] { return set_cell(*b->eng, cell_m); });

@@ -47,6 +47,7 @@
 #include "flock_engine.h"
 #include "flock_params.h"
 #include "k_decide.cuh"
+#include "k_decide_staged.cuh"
 #include "k_fp64.cuh"
 #include "k_grid.cuh"
 #include "k_integrate.cuh"
@@ -66,6 +67,7 @@ const char* device_error_text(uint32_t word) {
         case DEV_OK: return "no device error";
         case DEV_SCAN_TIMEOUT: return "a scan look-back wait gave up (error word 1)";
         case DEV_BAD_RANGE: return "a bucket range or slot fell outside its array and was skipped (error word 2)";
+        case DEV_STAGE_TIMEOUT: return "a staged decide's bulk copies did not land in time (error word 3)";
         default: return "unknown device error word";
     }
 }
@@ -152,15 +154,23 @@ size_t Engine::bytes_for(uint32_t n) {
     return (size_t)n * (136 + 88) + b * 16 + (b / SCAN_TILE) * 8 + 256;
 }
 
+// staged positions a k_decide_staged CTA holds
+static constexpr uint32_t STAGE_CAP = 4096;
+
 size_t Engine::decide_smem(bool sets) const {
-    const size_t w = (size_t)(shape_.decide_threads / 32);
-    return w * (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>()) + shape_.decide_extra_smem;
+    const int w = shape_.decide_threads / 32;
+    if (!sets && shape_.decide_kind == 1) return staged_smem_bytes(w, STAGE_CAP) + shape_.decide_extra_smem;
+    return (size_t)w * (sets ? decide_smem_per_warp<true>() : decide_smem_per_warp<false>()) +
+           shape_.decide_extra_smem;
 }
 
 void Engine::decide_occupancy(int* blocks_per_sm, int* threads, size_t* smem_bytes) const {
     const size_t smem = decide_smem(false);
     int n = 0;
-    FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decide<false>, shape_.decide_threads, smem));
+    if (shape_.decide_kind == 1)
+        FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decide_staged, shape_.decide_threads, smem));
+    else
+        FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decide<false>, shape_.decide_threads, smem));
     *blocks_per_sm = n;
     *threads = shape_.decide_threads;
     *smem_bytes = smem;
@@ -170,7 +180,9 @@ void Engine::set_shape(const LaunchShape& s) {
     int optin = 0;
     FLK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
     const size_t w = (size_t)(s.decide_threads / 32);
-    const size_t need = std::max(w * decide_smem_per_warp<false>(), w * decide_smem_per_warp<true>()) +
+    if (s.decide_kind != 0 && s.decide_kind != 1) throw Error{-1, "decide kind must be 0 (direct) or 1 (staged)"};
+    const size_t need = std::max({w * decide_smem_per_warp<false>(), w * decide_smem_per_warp<true>(),
+                                  s.decide_kind == 1 ? staged_smem_bytes((int)w, STAGE_CAP) : (size_t)0}) +
                         s.decide_extra_smem;
     if (need > (size_t)optin)
         throw Error{-1, "decide would need " + std::to_string(need) + " B of shared memory per CTA, above the " +
@@ -182,6 +194,9 @@ void Engine::set_shape(const LaunchShape& s) {
                                   (int)decide_smem(false)));
     FLK_CUDA(cudaFuncSetAttribute(k_decide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)decide_smem(true)));
+    if (s.decide_kind == 1)
+        FLK_CUDA(cudaFuncSetAttribute(k_decide_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)decide_smem(false)));
     auto fit = [](auto kernel) {
         int n = 0;
         FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0));
@@ -696,6 +711,10 @@ void Engine::enqueue_step(bool sets, cudaEvent_t* ev, bool f64, int buf, bool ha
         k_decide<true><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                        g.counts, ar_, sfwd_, radius_table_, sets_,
                                                                        slabs_, GRID_CELL, INV_CELL);
+    else if (shape_.decide_kind == 1)
+        k_decide_staged<<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
+                                                                            g.counts, ar_, sfwd_, radius_table_,
+                                                                            slabs_, cell, inv_cell, STAGE_CAP);
     else
         k_decide<false><<<dblocks, shape_.decide_threads, qbytes, stream_>>>(table_d_, nfl, V_, ctl_, due_, offsets_,
                                                                         g.counts, ar_, sfwd_, radius_table_, nullptr,

@@ -88,6 +88,7 @@ enum DeviceError : uint32_t {
     DEV_OK = 0,
     DEV_SCAN_TIMEOUT = 1,  // a scan look-back wait gave up
     DEV_BAD_RANGE = 2,     // a bucket range or slot fell outside its array (skipped, not accessed)
+    DEV_STAGE_TIMEOUT = 3, // a staged decide's bulk copies did not land within the wait limit
 };
 
 // Per-pass timing of a step, mean ms over the timed steps (reference's table).
@@ -106,6 +107,7 @@ struct LaunchShape {
     int graph_chunk = 10;           // steps per captured CUDA graph
     size_t decide_extra_smem = 0;   // dynamic shared memory reserved beyond decide's own (occupancy experiments)
     float cell = 4.0f;              // production cell edge (m); any edge gives the same neighbour sets
+    int decide_kind = 0;            // production decide: 0 sweeps the state, 1 stages cells in shared memory
 };
 
 struct GridDebug {  // host copies of one step's grid and neighbour-set summaries

@@ -87,13 +87,22 @@ struct Sweep {
     Acc a;
 };
 
-// Expensive phase for one hit t (d2 <= c2 already established).
-template <bool SETS>
+// A candidate's position: from the state through the read-only cache, or
+// (STG) from positions the CTA staged in shared memory.
+template <bool STG>
+__device__ __forceinline__ float4 ldpos(const float4* p) {
+    if (STG) return *p;
+    return __ldg(p);
+}
+
+// Expensive phase for one hit t (d2 <= c2 already established). STG: t is an
+// index into the staged positions, whose .w holds the candidate's view index.
+template <bool SETS, bool STG = false>
 __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
-    const float4 q = __ldg(&w.pos[t + w.shift]);
+    const float4 q = ldpos<STG>(&w.pos[t + w.shift]);
     // the neighbour's heading is needed only inside the blind cone, but
     // loading it here, before the arithmetic, hides the load's latency
-    const float4 fw = __ldg(&w.sfwd[t]);
+    const float4 fw = __ldg(&w.sfwd[STG ? __float_as_uint(q.w) : t]);
     const f3 d = mk(__fsub_rn(q.x, w.p.x), __fsub_rn(q.y, w.p.y), __fsub_rn(q.z, w.p.z));
     const float d2 = dot(d, d);
     const float dist = __fsqrt_rn(d2);
@@ -124,7 +133,7 @@ __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
 }
 
 // Queues the lanes' hits; when 32 are waiting, the whole warp takes them.
-template <bool SETS>
+template <bool SETS, bool STG = false>
 __device__ __forceinline__ void enqueue(Sweep& w, bool hit, uint32_t t, uint32_t lane) {
     const uint32_t hm = __ballot_sync(FULL, hit);
     if (!hm) return;
@@ -132,7 +141,7 @@ __device__ __forceinline__ void enqueue(Sweep& w, bool hit, uint32_t t, uint32_t
     w.qn += __popc(hm);
     if (w.qn >= 32) {
         __syncwarp();
-        take<SETS>(w, w.q[lane]);
+        take<SETS, STG>(w, w.q[lane]);
         const uint32_t extra = w.qn - 32;
         const uint32_t moved = lane < extra ? w.q[32 + lane] : 0u;
         __syncwarp();
@@ -145,7 +154,7 @@ __device__ __forceinline__ void enqueue(Sweep& w, bool hit, uint32_t t, uint32_t
 // Queues two chunks' hits at once (A's, then B's, the order of two single
 // enqueues) and takes full batches of 32. Hit k of the bird still goes to lane
 // k mod 32, so the sums are the same as with one chunk per enqueue.
-template <bool SETS>
+template <bool SETS, bool STG = false>
 __device__ __forceinline__ void enqueue2(Sweep& w, bool hA, uint32_t tA, bool hB, uint32_t tB, uint32_t lane) {
     const uint32_t ma = __ballot_sync(FULL, hA), mb = __ballot_sync(FULL, hB);
     if (!(ma | mb)) return;
@@ -155,7 +164,7 @@ __device__ __forceinline__ void enqueue2(Sweep& w, bool hA, uint32_t tA, bool hB
     w.qn += na + __popc(mb);
     while (w.qn >= 32) {
         __syncwarp();
-        take<SETS>(w, w.q[lane]);
+        take<SETS, STG>(w, w.q[lane]);
         const uint32_t extra = w.qn - 32;
         const uint32_t m0 = lane < extra ? w.q[32 + lane] : 0u;
         const uint32_t m1 = lane + 32 < extra ? w.q[64 + lane] : 0u;
@@ -208,7 +217,7 @@ __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32
 // exactly the order of a range-by-range sweep, so the hit queue, and every
 // sum, is unchanged; short ranges just stop wasting lanes. A lane finds the
 // range of its candidate i from the bitmask of ranges starting in its chunk.
-template <bool SETS>
+template <bool SETS, bool STG = false>
 __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, uint32_t lane) {
     const uint32_t nz = __ballot_sync(FULL, e > s);
     const uint32_t R = __popc(nz);
@@ -242,21 +251,21 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
         r0 += __popc(bA) + __popc(bB);
         const bool vA = iA < T && tA != w.self, vB = iB < T && tB != w.self;
         // invalid lanes read the bird's own slot (always in range) and discard it
-        const float4 qA = __ldg(&w.pos[(vA ? tA : w.self) + w.shift]);
-        const float4 qB = __ldg(&w.pos[(vB ? tB : w.self) + w.shift]);
+        const float4 qA = ldpos<STG>(&w.pos[(vA ? tA : w.self) + w.shift]);
+        const float4 qB = ldpos<STG>(&w.pos[(vB ? tB : w.self) + w.shift]);
         bool hA, hB;
         near2(w, qA, qB, hA, hB);
         hA = hA && vA;
         hB = hB && vB;
-        enqueue2<SETS>(w, hA, tA, hB, tB, lane);
+        enqueue2<SETS, STG>(w, hA, tA, hB, tB, lane);
     }
 }
 
-template <bool SETS>
+template <bool SETS, bool STG = false>
 __device__ __forceinline__ void drain(Sweep& w, uint32_t lane) {
     if (w.qn) {
         __syncwarp();
-        if (lane < w.qn) take<SETS>(w, w.q[lane]);
+        if (lane < w.qn) take<SETS, STG>(w, w.q[lane]);
         __syncwarp();
         w.qn = 0;
     }
@@ -407,23 +416,223 @@ __device__ __forceinline__ uint32_t bucket_of(int cx, int cy, int cz, uint32_t b
     return SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u)) : lattice_bucket(cx, cy, cz, buckets);
 }
 
+// Sets up the sweep of one deciding bird from its record.
+__device__ __forceinline__ void start_bird(Sweep& w, const DueRec& rec) {
+    const float r = rec.pr.w;
+    w.shift = rec.fl.w;
+    w.p = mk(rec.pr.x, rec.pr.y, rec.pr.z);
+    w.fi = mk(rec.fk.x, rec.fk.y, rec.fk.z);
+    w.r2 = __fmul_rn(r, r);
+    const float rr = __fmul_rn(2.0f, r);
+    w.c2 = __fmul_rn(rr, rr);
+    w.self = __float_as_uint(rec.fk.w);
+    w.a.sep = w.a.coh = w.a.align = w.a.csum = mk(0.f, 0.f, 0.f);
+    w.a.n_all = w.a.n_star = w.a.n_align = w.a.n_g = 0;
+    w.a.h_all = w.a.h_star = w.a.h_align = w.a.h_g = 0;
+}
+
+// Sweeps one deciding bird's neighbourhood from the state (record rec, its
+// box from group_boxes in slot `slot` of the warp's shared memory), queueing
+// and taking its hits; cells of edge `cell` (1 / inv_cell).
+template <bool SETS>
+__device__ __forceinline__ void sweep_bird(Sweep& w, const WarpSmem<SETS>& m, uint32_t slot, const DueRec& rec,
+                                           const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                           StepCtl* __restrict__ ctl, const uint32_t* __restrict__ offsets,
+                                           const uint32_t* __restrict__ counts, const Arena& ar,
+                                           const uint32_t* __restrict__ slabs, float cell, float inv_cell,
+                                           uint32_t lane, uint32_t& cand) {
+    const int4 box = m.box[slot];
+    const uint4 aux = m.aux[slot];
+    const uint32_t k = __float_as_uint(rec.fk.w), bbase = rec.fl.y, buckets = rec.fl.z;
+    const float r = rec.pr.w;
+    const f3 p = w.p;
+    if (aux.w >> 31) {
+        // fast path (search box of at most 32 cells, from group_boxes): each
+        // distinct bucket of the culled box once, no cell check
+        const float reach2 = __uint_as_float(aux.x);
+        const uint32_t nx = aux.y >> 17, ny = aux.z >> 17;
+        const int lx = box.x, ly = box.y, zlo = box.z, zhi = box.w;
+        const int2 zc = m.zc[slot];
+        const int lz = zc.x;
+        const uint32_t ncell = nx * ny * (uint32_t)zc.y;
+        bool valid = false;
+        uint32_t b = 0;
+        int z0 = 0, z1 = 3;  // production steps: the z-slabs of this lane's cell within reach
+        if (lane < ncell) {
+            // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift (div_magic)
+            const uint32_t t = (lane * (aux.y & 0x1FFFFu)) >> 16;
+            const uint32_t iz = (t * (aux.z & 0x1FFFFu)) >> 16;
+            const int cx = lx + (int)(lane - t * nx);
+            const int cy = ly + (int)(t - iz * ny), cz = lz + (int)iz;
+            if (!SETS) {
+                z0 = min(3, max(0, zlo - 4 * cz));
+                z1 = min(3, max(0, zhi - 4 * cz));
+            }
+            const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
+            const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
+            const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
+            const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
+            valid = dx * dx + dy * dy + dz * dz <= reach2;
+            b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
+                              : lattice_bucket_bits(cx, cy, cz, aux.w));
+        }
+        const uint32_t vm = __ballot_sync(FULL, valid);
+        bool keep = false;
+        if (valid) {
+            const uint32_t peers = __match_any_sync(vm, b);
+            keep = (int)lane == __ffs(peers) - 1;
+        }
+        uint32_t s = 0, en = 0;
+        if (keep) {
+            // Production runs are ordered by quarter-cell z-slab within their
+            // cell, and the sort left each run's slab boundaries (birds in slabs
+            // < 1, < 2, < 3; 10 bits each; all ones: untrimmed). A candidate
+            // within the reach has |dz| <= reach and floor is monotonic, so only
+            // slabs z0..z1 of this cell can hold one: the range shrinks to them.
+            // (The trim takes the bucket's cell to be this lane's: no two cells of
+            // the box share a bucket in production steps, since the box spans at
+            // most 3 cells per axis and the lattice index repeats only every 16
+            // cells or more.)
+            const uint32_t sw = SETS ? 0xFFFFFFFFu : __ldg(&slabs[b]);  // issued with the range's loads
+            bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
+            if (!SETS && en > s && sw != 0xFFFFFFFFu) {
+                const uint32_t L = en - s;
+                const uint32_t lo = z0 <= 0 ? 0u : (sw >> (10 * (z0 - 1))) & 1023u;
+                const uint32_t hi = z1 >= 3 ? L : (sw >> (10 * z1)) & 1023u;
+                if (hi <= L) {  // else a stale word: keep the run whole
+                    if (lo >= hi) {
+                        en = s;
+                    } else {
+                        en = s + hi;
+                        s += lo;
+                    }
+                }
+            }
+        }
+        cand += en - s;
+        sweep_packed<SETS>(w, s, en, lane);
+    } else {
+        const SearchBox sb = search_box(p, r, inv_cell);
+        const float reach2 = sb.reach2;
+        const int lx = sb.lx, ly = sb.ly, lz = sb.lz;
+        const long long nxl = sb.nx, nyl = sb.ny, ncell = sb.ncell;
+        // the flock's own view region [vbase, vbase + n)
+        const FlockDesc* fd = &fl[find_flock_v(fl, nfl, k)];
+        uint32_t f0 = __ldg(&fd->vbase), f1 = f0 + __ldg(&fd->n);
+        const uint32_t sf = f0 + w.shift;
+        if (f1 < f0 || f1 > V || sf + (f1 - f0) < sf || sf + (f1 - f0) > 2u * ar.cap) f1 = f0 = 0;
+        if (ncell * 16 >= (long long)(f1 - f0)) {
+            // very wide reach: brute force over the flock's own range
+            if (lane == 0) cand += f1 - f0;
+            sweep<SETS, false>(w, f0, f1, lane);
+        } else {
+            // cell walk with the exact cell check (buckets may repeat)
+            for (long long c0 = 0; c0 < ncell; c0 += 32) {
+                const long long ci = c0 + lane;
+                bool valid = false;
+                int cx = 0, cy = 0, cz = 0;
+                uint32_t s = 0, en = 0;
+                if (ci < ncell) {
+                    cx = lx + (int)(ci % nxl);
+                    const long long t = ci / nxl;
+                    cy = ly + (int)(t % nyl);
+                    cz = lz + (int)(t / nyl);
+                    const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
+                    const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
+                    const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
+                    const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
+                    valid = dx * dx + dy * dy + dz * dz <= reach2;
+                    if (valid) {
+                        bucket_range(offsets, counts, bbase + bucket_of<SETS>(cx, cy, cz, buckets), V, w.shift,
+                                     2u * ar.cap, ctl, s, en);
+                        valid = en > s;
+                    }
+                }
+                cand += en - s;
+                uint32_t km = __ballot_sync(FULL, valid);
+                while (km) {
+                    const int c = __ffs(km) - 1;
+                    km &= km - 1;
+                    const uint32_t sc = __shfl_sync(FULL, s, c), ec = __shfl_sync(FULL, en, c);
+                    const int ccx = __shfl_sync(FULL, cx, c), ccy = __shfl_sync(FULL, cy, c),
+                              ccz = __shfl_sync(FULL, cz, c);
+                    sweep<SETS, true>(w, sc, ec, lane, ccx, ccy, ccz, inv_cell);
+                }
+            }
+        }
+    }
+    drain<SETS>(w, lane);
+}
+
+// Reduces the warp's sums for the current bird (slot `slot` of the batch, its
+// slot st in the state, view index k, height pz) and runs the batch's
+// epilogue once 32 birds wait.
+template <bool SETS>
+__device__ __forceinline__ void finish_bird(Sweep& w, WarpSmem<SETS>& m, uint32_t& slot, uint32_t st, uint32_t k,
+                                            float pz, const Arena& ar, const float* __restrict__ rtab,
+                                            uint32_t* __restrict__ sets, uint32_t lane, uint32_t& pairs) {
+    {
+        float fv[16] = {w.a.sep.x,   w.a.sep.y,   w.a.sep.z,   w.a.coh.x,  w.a.coh.y,  w.a.coh.z,
+                        w.a.align.x, w.a.align.y, w.a.align.z, w.a.csum.x, w.a.csum.y, w.a.csum.z,
+                        0.f,         0.f,         0.f,         0.f};
+        const float tf = rs_float<16>(fv, lane);
+        if ((lane & 1) == 0) m.red[(lane >> 1) & 15][slot] = tf;
+    }
+    if (SETS) {
+        uint32_t iv[8] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g, w.a.h_all, w.a.h_star, w.a.h_align, w.a.h_g};
+        const uint32_t ti = rs_uint<8>(iv, lane);
+        if ((lane & 3) == 0) m.cnt[(lane >> 2) & 7][slot] = ti;
+        if (lane == 12) pairs += ti;  // lane 12 holds n_g
+    } else {
+        uint32_t iv[4] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g};
+        const uint32_t ti = rs_uint<4>(iv, lane);
+        if ((lane & 7) == 0) m.cnt[(lane >> 3) & 3][slot] = ti;
+        if (lane == 24) pairs += ti;  // lane 24 holds n_g
+    }
+    if (lane == 0) {
+        m.st[slot] = st;
+        m.vix[slot] = k;
+        m.pz[slot] = pz;
+    }
+    if (++slot == 32) {
+        __syncwarp();
+        epilogue<SETS>(m, lane, ar, rtab, sets);
+        __syncwarp();
+        slot = 0;
+    }
+}
+
+// The batch's last birds, and the per-warp counter totals (no block barrier).
+template <bool SETS>
+__device__ __forceinline__ void finish_warp(WarpSmem<SETS>& m, uint32_t slot, const Arena& ar,
+                                            const float* __restrict__ rtab, uint32_t* __restrict__ sets,
+                                            uint32_t lane, bool counts_due, uint32_t ndue, uint32_t cand,
+                                            uint32_t pairs, StepCtl* __restrict__ ctl) {
+    if (slot) {
+        __syncwarp();
+        if (lane < slot) epilogue<SETS>(m, lane, ar, rtab, sets);
+    }
+    const uint32_t cand_w = __reduce_add_sync(FULL, cand), pairs_w = __reduce_add_sync(FULL, pairs);
+    if (lane == 0) {
+        if (cand_w) atomicAdd(&ctl->cand_total, (unsigned long long)cand_w);
+        if (pairs_w) atomicAdd(&ctl->pair_total, (unsigned long long)pairs_w);
+        if (counts_due) atomicAdd(&ctl->due_total, (unsigned long long)ndue);
+    }
+}
+
 // Dynamic shared memory: one WarpSmem<SETS> per warp. 64 registers per
 // thread, so one 1024-thread CTA fills an SM; with that shape all 32 warps of
 // an SM take consecutive due records, i.e. neighbouring birds, and share their
 // candidates in L1 (0.221 -> 0.203 ms at 1M birds against four 256-thread
 // CTAs per SM, which take records from four distant places).
 template <bool SETS>
-__global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict__ fl, int nfl,
-                                                                      uint32_t V, StepCtl* __restrict__ ctl,
-                                                                      const DueRec* __restrict__ due,
-                                                                      const uint32_t* __restrict__ offsets,
-                                                                      const uint32_t* __restrict__ counts,
-                                                                      Arena ar,
-                                                                      const float4* __restrict__ sfwd,
-                                                                      const float* __restrict__ rtab,
-                                                                      uint32_t* __restrict__ sets,
-                                                                      const uint32_t* __restrict__ slabs,
-                                                                      float pcell_edge, float pinv_cell) {
+__global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict__ fl, int nfl, uint32_t V,
+                                                    StepCtl* __restrict__ ctl, const DueRec* __restrict__ due,
+                                                    const uint32_t* __restrict__ offsets,
+                                                    const uint32_t* __restrict__ counts, Arena ar,
+                                                    const float4* __restrict__ sfwd, const float* __restrict__ rtab,
+                                                    uint32_t* __restrict__ sets, const uint32_t* __restrict__ slabs,
+                                                    float pcell_edge, float pinv_cell) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     WarpSmem<SETS>& m = reinterpret_cast<WarpSmem<SETS>*>(s_raw)[threadIdx.x >> 5];
     const uint32_t lane = threadIdx.x & 31;
@@ -443,185 +652,12 @@ __global__ void __launch_bounds__(1024, 1) k_decide(const FlockDesc* __restrict_
 
     for (uint32_t e = gw; e < ndue; e += nw) {
         if (slot == 0) group_boxes<SETS>(m, due, e, nw, ndue, lane, inv_cell);
-        const int4 box = m.box[slot];
-        const uint4 aux = m.aux[slot];
         const DueRec rec = due[e];  // everything the setup needs, one place
-        const uint32_t k = __float_as_uint(rec.fk.w);
-        const uint32_t st = rec.fl.x, bbase = rec.fl.y, buckets = rec.fl.z;
-        w.shift = rec.fl.w;
-        const float r = rec.pr.w;
-        w.p = mk(rec.pr.x, rec.pr.y, rec.pr.z);
-        w.fi = mk(rec.fk.x, rec.fk.y, rec.fk.z);
-        w.r2 = __fmul_rn(r, r);
-        const float rr = __fmul_rn(2.0f, r);
-        w.c2 = __fmul_rn(rr, rr);
-        w.self = k;
-        const f3 p = w.p;
-
-        w.a.sep = w.a.coh = w.a.align = w.a.csum = mk(0.f, 0.f, 0.f);
-        w.a.n_all = w.a.n_star = w.a.n_align = w.a.n_g = 0;
-        w.a.h_all = w.a.h_star = w.a.h_align = w.a.h_g = 0;
-
-        if (aux.w >> 31) {
-            // fast path (search box of at most 32 cells, from group_boxes): each
-            // distinct bucket of the culled box once, no cell check
-            const float reach2 = __uint_as_float(aux.x);
-            const uint32_t nx = aux.y >> 17, ny = aux.z >> 17;
-            const int lx = box.x, ly = box.y, zlo = box.z, zhi = box.w;
-            const int2 zc = m.zc[slot];
-            const int lz = zc.x;
-            const uint32_t ncell = nx * ny * (uint32_t)zc.y;
-            bool valid = false;
-            uint32_t b = 0;
-            int z0 = 0, z1 = 3;  // production steps: the z-slabs of this lane's cell within reach
-            if (lane < ncell) {
-                // lane = ix + nx * (iy + ny * iz), quotients by multiply-shift (div_magic)
-                const uint32_t t = (lane * (aux.y & 0x1FFFFu)) >> 16;
-                const uint32_t iz = (t * (aux.z & 0x1FFFFu)) >> 16;
-                const int cx = lx + (int)(lane - t * nx);
-                const int cy = ly + (int)(t - iz * ny), cz = lz + (int)iz;
-                if (!SETS) {
-                    z0 = min(3, max(0, zlo - 4 * cz));
-                    z1 = min(3, max(0, zhi - 4 * cz));
-                }
-                const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
-                const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
-                const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
-                const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
-                valid = dx * dx + dy * dy + dz * dz <= reach2;
-                b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
-                                  : lattice_bucket_bits(cx, cy, cz, aux.w));
-            }
-            const uint32_t vm = __ballot_sync(FULL, valid);
-            bool keep = false;
-            if (valid) {
-                const uint32_t peers = __match_any_sync(vm, b);
-                keep = (int)lane == __ffs(peers) - 1;
-            }
-            uint32_t s = 0, en = 0;
-            if (keep) {
-                // Production runs are ordered by quarter-cell z-slab within their
-                // cell, and the sort left each run's slab boundaries (birds in slabs
-                // < 1, < 2, < 3; 10 bits each; all ones: untrimmed). A candidate
-                // within the reach has |dz| <= reach and floor is monotonic, so only
-                // slabs z0..z1 of this cell can hold one: the range shrinks to them.
-                // (The trim takes the bucket's cell to be this lane's: no two cells of
-                // the box share a bucket in production steps, since the box spans at
-                // most 3 cells per axis and the lattice index repeats only every 16
-                // cells or more.)
-                const uint32_t sw = SETS ? 0xFFFFFFFFu : __ldg(&slabs[b]);  // issued with the range's loads
-                bucket_range(offsets, counts, b, V, w.shift, 2u * ar.cap, ctl, s, en);
-                if (!SETS && en > s && sw != 0xFFFFFFFFu) {
-                    const uint32_t L = en - s;
-                    const uint32_t lo = z0 <= 0 ? 0u : (sw >> (10 * (z0 - 1))) & 1023u;
-                    const uint32_t hi = z1 >= 3 ? L : (sw >> (10 * z1)) & 1023u;
-                    if (hi <= L) {  // else a stale word: keep the run whole
-                        if (lo >= hi) {
-                            en = s;
-                        } else {
-                            en = s + hi;
-                            s += lo;
-                        }
-                    }
-                }
-            }
-            cand += en - s;
-            sweep_packed<SETS>(w, s, en, lane);
-        } else {
-            const SearchBox sb = search_box(p, r, inv_cell);
-            const float reach2 = sb.reach2;
-            const int lx = sb.lx, ly = sb.ly, lz = sb.lz;
-            const long long nxl = sb.nx, nyl = sb.ny, ncell = sb.ncell;
-            // the flock's own view region [vbase, vbase + n)
-            const FlockDesc* fd = &fl[find_flock_v(fl, nfl, k)];
-            uint32_t f0 = __ldg(&fd->vbase), f1 = f0 + __ldg(&fd->n);
-            const uint32_t sf = f0 + w.shift;
-            if (f1 < f0 || f1 > V || sf + (f1 - f0) < sf || sf + (f1 - f0) > 2u * ar.cap) f1 = f0 = 0;
-            if (ncell * 16 >= (long long)(f1 - f0)) {
-                // very wide reach: brute force over the flock's own range
-                if (lane == 0) cand += f1 - f0;
-                sweep<SETS, false>(w, f0, f1, lane);
-            } else {
-                // cell walk with the exact cell check (buckets may repeat)
-                for (long long c0 = 0; c0 < ncell; c0 += 32) {
-                    const long long ci = c0 + lane;
-                    bool valid = false;
-                    int cx = 0, cy = 0, cz = 0;
-                    uint32_t s = 0, en = 0;
-                    if (ci < ncell) {
-                        cx = lx + (int)(ci % nxl);
-                        const long long t = ci / nxl;
-                        cy = ly + (int)(t % nyl);
-                        cz = lz + (int)(t / nyl);
-                        const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
-                        const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
-                        const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
-                        const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
-                        valid = dx * dx + dy * dy + dz * dz <= reach2;
-                        if (valid) {
-                            bucket_range(offsets, counts, bbase + bucket_of<SETS>(cx, cy, cz, buckets), V, w.shift,
-                                         2u * ar.cap, ctl, s, en);
-                            valid = en > s;
-                        }
-                    }
-                    cand += en - s;
-                    uint32_t km = __ballot_sync(FULL, valid);
-                    while (km) {
-                        const int c = __ffs(km) - 1;
-                        km &= km - 1;
-                        const uint32_t sc = __shfl_sync(FULL, s, c), ec = __shfl_sync(FULL, en, c);
-                        const int ccx = __shfl_sync(FULL, cx, c), ccy = __shfl_sync(FULL, cy, c),
-                                  ccz = __shfl_sync(FULL, cz, c);
-                        sweep<SETS, true>(w, sc, ec, lane, ccx, ccy, ccz, inv_cell);
-                    }
-                }
-            }
-        }
-        drain<SETS>(w, lane);
-
-        // reduce-scatter into this bird's slot of the batch
-        {
-            float fv[16] = {w.a.sep.x,  w.a.sep.y,   w.a.sep.z,   w.a.coh.x,  w.a.coh.y,  w.a.coh.z,
-                            w.a.align.x, w.a.align.y, w.a.align.z, w.a.csum.x, w.a.csum.y, w.a.csum.z,
-                            0.f,         0.f,         0.f,         0.f};
-            const float tf = rs_float<16>(fv, lane);
-            if ((lane & 1) == 0) m.red[(lane >> 1) & 15][slot] = tf;
-        }
-        if (SETS) {
-            uint32_t iv[8] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g,
-                              w.a.h_all, w.a.h_star, w.a.h_align, w.a.h_g};
-            const uint32_t ti = rs_uint<8>(iv, lane);
-            if ((lane & 3) == 0) m.cnt[(lane >> 2) & 7][slot] = ti;
-            if (lane == 12) pairs += ti;  // lane 12 holds n_g
-        } else {
-            uint32_t iv[4] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g};
-            const uint32_t ti = rs_uint<4>(iv, lane);
-            if ((lane & 7) == 0) m.cnt[(lane >> 3) & 3][slot] = ti;
-            if (lane == 24) pairs += ti;  // lane 24 holds n_g
-        }
-        if (lane == 0) {
-            m.st[slot] = st;
-            m.vix[slot] = k;
-            m.pz[slot] = p.z;
-        }
-        if (++slot == 32) {
-            __syncwarp();
-            epilogue<SETS>(m, lane, ar, rtab, sets);
-            __syncwarp();
-            slot = 0;
-        }
+        start_bird(w, rec);
+        sweep_bird<SETS>(w, m, slot, rec, fl, nfl, V, ctl, offsets, counts, ar, slabs, cell, inv_cell, lane, cand);
+        finish_bird<SETS>(w, m, slot, rec.fl.x, __float_as_uint(rec.fk.w), rec.pr.z, ar, rtab, sets, lane, pairs);
     }
-    if (slot) {
-        __syncwarp();
-        if (lane < slot) epilogue<SETS>(m, lane, ar, rtab, sets);
-    }
-    // per-warp totals straight to the counters (no block barrier)
-    const uint32_t cand_w = __reduce_add_sync(FULL, cand), pairs_w = __reduce_add_sync(FULL, pairs);
-    if (lane == 0) {
-        if (cand_w) atomicAdd(&ctl->cand_total, (unsigned long long)cand_w);
-        if (pairs_w) atomicAdd(&ctl->pair_total, (unsigned long long)pairs_w);
-        if (gw == 0) atomicAdd(&ctl->due_total, (unsigned long long)ndue);
-    }
+    finish_warp<SETS>(m, slot, ar, rtab, sets, lane, gw == 0, ndue, cand, pairs, ctl);
 }
 
 template <bool SETS>

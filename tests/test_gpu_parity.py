@@ -312,6 +312,59 @@ def test_production_cell_edges_decide_the_same(native, oracle, cell):
     g.close()
 
 
+def test_staged_decide_matches_the_oracle_and_the_direct_sweep(native, oracle):
+    # the cell-blocked decide (neighbourhood staged in shared memory by bulk
+    # copies) against the oracle from the same state, and against the direct
+    # sweep: the same decisions, states equal to rounding, one step and 20 on
+    w = native.generate(100_000, 1)
+    t_cpu, c, _, _ = oracle.step(w, 0.0)
+    a = native.Flock(w)
+    a.tune_decide(1)
+    a.step(1)
+    ta, wa = a.read()
+    assert ta == t_cpu
+    assert_state_parity(wa, c, oracle)
+    b = native.Flock(w)
+    b.step(1)
+    assert_same_decisions(wa, b.read()[1])
+    a.step(20)
+    b.step(20)
+    ok, maxes, mism, _ = oracle.diff(a.read()[1], b.read()[1])
+    assert ok and mism == 0, maxes
+    a.close()
+    b.close()
+
+
+def test_staged_decide_at_one_million_and_in_a_mixed_batch(native, oracle):
+    # 1M birds, 30 steps in: staged and direct decide alike; and a batch whose
+    # flocks meet inside one CTA's birds (the staged kernel sweeps those directly)
+    w = native.generate(1_000_000, 1)
+    f = native.Flock(w)
+    f.step(30)
+    _, s = f.read()
+    f.close()
+    outs = []
+    for staged in (1, 0):
+        g = native.Flock(s)
+        g.tune_decide(staged)
+        g.step(1)
+        outs.append(g.read()[1])
+        g.close()
+    assert_same_decisions(outs[0], outs[1])
+    flocks = [native.generate(n, 60 + k) for k, n in enumerate([1500, 40_000, 300, 9000, 120_000])]
+    res = []
+    for staged in (1, 0):
+        bt = native.Batch()
+        ids = [bt.add(x) for x in flocks]
+        bt.tune(staged=staged)
+        bt.step(12)
+        res.append([bt.read(i)[1] for i in ids])
+        bt.close()
+    for x, y in zip(*res):
+        ok, maxes, mism, _ = oracle.diff(x, y)
+        assert ok and mism == 0, maxes
+
+
 def test_wide_radii_take_the_cell_walk_and_brute_force_paths(native, oracle):
     w = oracle.scatter(4000, 11)
     w[:200, 8] = 5.0    # 2R = 10 m: > 32 cells, cell walk with the exact cell check
