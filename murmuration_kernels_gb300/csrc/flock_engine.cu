@@ -43,6 +43,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "flock_engine.h"
 #include "flock_params.h"
@@ -81,17 +83,104 @@ uint32_t buckets_for(uint32_t n) {
 // ---------------------------------------------------------------------------
 // host engine
 // ---------------------------------------------------------------------------
-template <class T>
-static T* dalloc(size_t n, size_t* acct) {
+// Device memory cache shared by every engine of the process, per device.
+// cudaMalloc of the large arrays and cudaFree (which synchronises the whole
+// device) cost more than a short run of steps, so an engine's blocks go back
+// to the cache when it releases them (after its streams have finished with
+// them) and the next engine that asks for a block of the same rounded size
+// on that device takes it. At most CACHE_CAP bytes stay cached per device;
+// beyond that, blocks are freed.
+namespace {
+constexpr int CACHE_DEVICES = 64;
+constexpr size_t CACHE_CAP = 16ull << 30;
+struct DevCache {
+    std::mutex mu;
+    std::multimap<size_t, void*> free_blocks;  // rounded size -> block
+    std::map<void*, size_t> sizes;             // every block handed out: its rounded size
+    size_t cached = 0;
+};
+DevCache g_cache[CACHE_DEVICES];
+
+size_t round_bytes(size_t b) {
+    const size_t g = b <= (1u << 20) ? 4096 : (2u << 20);
+    return (b + g - 1) / g * g;
+}
+
+void* cache_alloc(int dev, size_t bytes) {
+    const size_t rb = round_bytes(std::max<size_t>(bytes, 1));
+    DevCache& c = g_cache[dev % CACHE_DEVICES];
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        auto it = c.free_blocks.find(rb);
+        if (it != c.free_blocks.end()) {
+            void* p = it->second;
+            c.free_blocks.erase(it);
+            c.cached -= rb;
+            return p;
+        }
+    }
     void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, rb);
+    if (e == cudaErrorMemoryAllocation) {
+        (void)cudaGetLastError();
+        // give the cached blocks back and try once more
+        std::lock_guard<std::mutex> lk(c.mu);
+        for (auto& kv : c.free_blocks) {
+            cudaFree(kv.second);
+            c.sizes.erase(kv.second);
+        }
+        c.free_blocks.clear();
+        c.cached = 0;
+        e = cudaMalloc(&p, rb);
+    }
+    if (e != cudaSuccess) throw Error{-3, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.sizes[p] = rb;
+    return p;
+}
+
+// The caller guarantees that no work in flight uses p.
+void cache_free(int dev, void* p) {
+    if (!p) return;
+    DevCache& c = g_cache[dev % CACHE_DEVICES];
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.sizes.find(p);
+    if (it == c.sizes.end()) return;  // never for a block from cache_alloc
+    const size_t rb = it->second;
+    if (c.cached + rb > CACHE_CAP) {
+        cudaFree(p);
+        c.sizes.erase(it);
+        return;
+    }
+    c.free_blocks.emplace(rb, p);
+    c.cached += rb;
+}
+
+// Per device, set up once for the process: the radius factor table
+// (params.rs:61-65 evaluated with the host libm, 65,536 powf calls) and the
+// streaming kernels' resident CTAs per SM.
+struct DevStatic {
+    std::once_flag once;
+    float* radius_table = nullptr;
+    int fit[10] = {};
+};
+DevStatic g_static[CACHE_DEVICES];
+}  // namespace
+
+template <class T>
+T* Engine::dalloc(size_t n, size_t* acct) {
     if (n == 0) n = 1;
-    FLK_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    void* p = cache_alloc(device_, n * sizeof(T));
     *acct += n * sizeof(T);
     return static_cast<T*>(p);
 }
 template <class T>
-static void dfree(T*& p) {
-    if (p) cudaFree(p);
+void Engine::dfree(T*& p) {
+    if (!p) return;
+    // the engine's queued work may still use the block: let it finish first
+    cudaStreamSynchronize(stream_);
+    cudaStreamSynchronize(copy_);
+    cache_free(device_, p);
     p = nullptr;
 }
 
@@ -106,13 +195,27 @@ Engine::Engine(int device) {
     StepCtl c{};
     c.epoch = 1;
     FLK_CUDA(cudaMemcpyAsync(ctl_, &c, sizeof c, cudaMemcpyHostToDevice, stream_));
-    std::vector<float> tab(RADIUS_TABLE);
-    for (int n = 0; n < RADIUS_TABLE; ++n) {
-        const float nn = (float)(n > 1 ? n : 1);
-        tab[n] = powf(N_C / nn, RADIUS_EXP);
-    }
-    radius_table_ = dalloc<float>(RADIUS_TABLE, &dev_bytes_);
-    FLK_CUDA(cudaMemcpyAsync(radius_table_, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, stream_));
+    DevStatic& ds = g_static[device_ % CACHE_DEVICES];
+    std::call_once(ds.once, [&] {
+        std::vector<float> tab(RADIUS_TABLE);
+        for (int n = 0; n < RADIUS_TABLE; ++n) {
+            const float nn = (float)(n > 1 ? n : 1);
+            tab[n] = powf(N_C / nn, RADIUS_EXP);
+        }
+        FLK_CUDA(cudaMalloc(&ds.radius_table, RADIUS_TABLE * sizeof(float)));  // held for the process
+        FLK_CUDA(cudaMemcpy(ds.radius_table, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+        auto fit = [](auto kernel) {
+            int n = 0;
+            FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0));
+            return std::max(1, n);
+        };
+        const int f[10] = {fit(k_hash_count<false>), fit(k_hash_count<true>), fit(k_place),     fit(k_scatter),
+                           fit(k_segsort),           fit(k_integrate<false>), fit(k_integrate<true>),
+                           fit(k_decide_f64),        fit(k_integrate_f64),  fit(k_compare_f64)};
+        std::copy(f, f + 10, ds.fit);
+    });
+    if (!ds.radius_table) throw Error{-3, "radius table set-up failed on this device"};
+    radius_table_ = ds.radius_table;
     FLK_CUDA(cudaStreamSynchronize(stream_));
     set_shape(shape_);  // decide's shared memory may exceed the default 48 KB per CTA
 }
@@ -127,7 +230,7 @@ Engine::~Engine() {
     dfree(key_); dfree(arrival_); dfree(tmp_); dfree(occ_); dfree(occ2_); dfree(due_);
     dfree(counts2_);
     dfree(sfwd_); dfree(counts_); dfree(offsets_); dfree(status_); dfree(sets_); dfree(slabs_);
-    dfree(ctl_); dfree(radius_table_); dfree(staging_);
+    dfree(ctl_); dfree(staging_);
     dfree(dec64_); dfree(out64_); dfree(active_); dfree(err64_);
     if (copy_) cudaStreamDestroy(copy_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -197,21 +300,18 @@ void Engine::set_shape(const LaunchShape& s) {
     if (s.decide_kind == 1)
         FLK_CUDA(cudaFuncSetAttribute(k_decide_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)decide_smem(false)));
-    auto fit = [](auto kernel) {
-        int n = 0;
-        FLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0));
-        return std::max(1, n);
-    };
-    fit_.hash[0] = fit(k_hash_count<false>);
-    fit_.hash[1] = fit(k_hash_count<true>);
-    fit_.place = fit(k_place);
-    fit_.scatter = fit(k_scatter);
-    fit_.segsort = fit(k_segsort);
-    fit_.integrate[0] = fit(k_integrate<false>);
-    fit_.integrate[1] = fit(k_integrate<true>);
-    fit_.decide_f64 = fit(k_decide_f64);
-    fit_.integrate_f64 = fit(k_integrate_f64);
-    fit_.compare_f64 = fit(k_compare_f64);
+    // the streaming kernels' resident CTAs per SM, queried once per device
+    const int* f = g_static[device_ % CACHE_DEVICES].fit;
+    fit_.hash[0] = f[0];
+    fit_.hash[1] = f[1];
+    fit_.place = f[2];
+    fit_.scatter = f[3];
+    fit_.segsort = f[4];
+    fit_.integrate[0] = f[5];
+    fit_.integrate[1] = f[6];
+    fit_.decide_f64 = f[7];
+    fit_.integrate_f64 = f[8];
+    fit_.compare_f64 = f[9];
     free_graphs();
 }
 
@@ -521,7 +621,8 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     if (table_h_.empty() || steps == 0) return;
     uint4* flush = nullptr;
     const size_t n16 = flush_bytes / 16;
-    if (n16) FLK_CUDA(cudaMalloc(&flush, n16 * 16));
+    size_t flush_acct = 0;
+    if (n16) flush = dalloc<uint4>(n16, &flush_acct);
     // Each timed step is one launch of a single-step graph that runs the step as
     // a multi-step run does: its integrate also counts the next step's grid, so
     // the step has no hash pass of its own. Steps alternate between the two grid
@@ -554,7 +655,7 @@ void Engine::time_steps_cold(uint32_t steps, size_t flush_bytes, float* ms_per_s
     for (uint32_t s = 0; s < steps; ++s) FLK_CUDA(cudaEventElapsedTime(&ms_per_step[s], ev[2 * s], ev[2 * s + 1]));
     for (auto& x : ev) cudaEventDestroy(x);
     for (auto& x : one) cudaGraphExecDestroy(x);
-    if (flush) cudaFree(flush);
+    dfree(flush);
     const uint32_t ran = steps + 1;
     for (size_t k = 0; k < table_h_.size(); ++k) {
         const uint32_t left = table_h_[k].remaining > ran ? table_h_[k].remaining - ran : 0;

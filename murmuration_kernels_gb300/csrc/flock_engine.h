@@ -198,6 +198,11 @@ public:
     static int kernels_per_step() { return 6; }
 
 private:
+    // device memory through the process-wide per-device cache
+    template <class T>
+    T* dalloc(size_t n, size_t* acct);
+    template <class T>
+    void dfree(T*& p);
     struct Slot {
         uint32_t n = 0, sbase = 0, buckets = 0, remaining = 0;
         uint32_t parity = 0;  // buffer holding the current state
