@@ -464,15 +464,23 @@ __device__ __forceinline__ void sweep_bird(Sweep& w, const WarpSmem<SETS>& m, ui
             const uint32_t iz = (t * (aux.z & 0x1FFFFu)) >> 16;
             const int cx = lx + (int)(lane - t * nx);
             const int cy = ly + (int)(t - iz * ny), cz = lz + (int)iz;
-            if (!SETS) {
-                z0 = min(3, max(0, zlo - 4 * cz));
-                z1 = min(3, max(0, zhi - 4 * cz));
-            }
             const float ox = (float)cx * cell, oy = (float)cy * cell, oz = (float)cz * cell;
             const float dx = fminf(fmaxf(p.x, ox), ox + cell) - p.x;
             const float dy = fminf(fmaxf(p.y, oy), oy + cell) - p.y;
             const float dz = fminf(fmaxf(p.z, oz), oz + cell) - p.z;
-            valid = dx * dx + dy * dy + dz * dz <= reach2;
+            const float dxy2 = dx * dx + dy * dy;
+            valid = dxy2 + dz * dz <= reach2;
+            if (!SETS) {
+                // The z-slabs of this cell that the sphere reaches: at the cell's
+                // nearest xy point the sphere spans |dz| <= sqrt(reach^2 - dxy^2)
+                // (dxy^2 a lower bound for any bird of the cell). The 1e-4 reach^2
+                // under the root, and the reach's own absolute margin, cover the
+                // rounding; the bird's whole z-range zlo..zhi bounds it.
+                const float hz = __fsqrt_rn(fmaxf(reach2 - dxy2, 0.f) + 1e-4f * reach2);
+                const float inv4 = __fmul_rn(4.0f, inv_cell);
+                z0 = min(3, max(0, max(zlo, pcell(p.z - hz, inv4)) - 4 * cz));
+                z1 = min(3, max(0, min(zhi, pcell(p.z + hz, inv4)) - 4 * cz));
+            }
             b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
                               : lattice_bucket_bits(cx, cy, cz, aux.w));
         }
