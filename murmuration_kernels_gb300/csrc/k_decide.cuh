@@ -95,8 +95,10 @@ __device__ __forceinline__ float4 ldpos(const float4* p) {
     return __ldg(p);
 }
 
-// Expensive phase for one hit t (d2 <= c2 already established). STG: t is an
-// index into the staged positions, whose .w holds the candidate's view index.
+// Expensive phase for one hit t: a member of the R set in production steps
+// (the sweep summed its 2R share, ring), of the 2R set in grid-reporting
+// steps (d2 <= c2 already established). STG: t is an index into the staged
+// positions, whose .w holds the candidate's view index.
 template <bool SETS, bool STG = false>
 __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
     const float4 q = ldpos<STG>(&w.pos[t + w.shift]);
@@ -107,11 +109,13 @@ __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
     const float d2 = dot(d, d);
     const float dist = __fsqrt_rn(d2);
     const f3 dh = dvs(d, fmaxf(dist, 1e-6f));
-    w.a.csum = add(w.a.csum, dh);
-    w.a.n_g += 1;
     const uint32_t j = SETS ? __ldg(&w.bid[t + w.shift]) : 0u;
-    if (SETS) w.a.h_g += set_mix(j);
-    if (d2 > w.r2) return;
+    if (SETS) {  // production steps add the 2R set's share in the sweep (ring) and queue only hits inside R
+        w.a.csum = add(w.a.csum, dh);
+        w.a.n_g += 1;
+        w.a.h_g += set_mix(j);
+        if (d2 > w.r2) return;
+    }
     w.a.n_all += 1;
     if (SETS) w.a.h_all += set_mix(j);
     float g = 1.0f;
@@ -176,27 +180,31 @@ __device__ __forceinline__ void enqueue2(Sweep& w, bool hA, uint32_t tA, bool hB
     }
 }
 
-// Cheap-phase test of candidate t; CHECK_CELL also requires cell (cx,cy,cz) of
-// edge 1 / inv_cell.
-template <bool CHECK_CELL>
-__device__ __forceinline__ bool near(const Sweep& w, const float4 q, int cx, int cy, int cz, float inv_cell) {
-    const float dx = __fsub_rn(q.x, w.p.x), dy = __fsub_rn(q.y, w.p.y), dz = __fsub_rn(q.z, w.p.z);
-    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    bool hit = d2 <= w.c2;
-    if (CHECK_CELL)
-        hit = hit && pcell(q.x, inv_cell) == cx && pcell(q.y, inv_cell) == cy && pcell(q.z, inv_cell) == cz;
-    return hit;
+// Offset d from the deciding bird to candidate position q, and |d|^2. Set
+// membership must round exactly as the oracle's chain of separately rounded
+// f32 operations, so the test stays in scalar round-to-nearest intrinsics:
+// paired f32x2 multiplies and adds (the __fmul2_rn/__fadd2_rn intrinsics, or
+// mul.rn/add.rn.f32x2 in PTX) were measured to round d2 differently, admitting
+// a bird one ulp outside 2R (test_two_birds_one_ulp_outside_2r), and cost no
+// time to give up.
+__device__ __forceinline__ float offset2(const Sweep& w, const float4 q, f3& d) {
+    d = mk(__fsub_rn(q.x, w.p.x), __fsub_rn(q.y, w.p.y), __fsub_rn(q.z, w.p.z));
+    return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
 }
 
-// near<false> for two candidates. Set membership must round exactly as the
-// oracle's chain of separately rounded f32 operations, so the test stays in
-// scalar round-to-nearest intrinsics: paired f32x2 multiplies and adds (the
-// __fmul2_rn/__fadd2_rn intrinsics, or mul.rn/add.rn.f32x2 in PTX) were
-// measured to round d2 differently, admitting a bird one ulp outside 2R
-// (test_two_birds_one_ulp_outside_2r), and cost no time to give up.
-__device__ __forceinline__ void near2(const Sweep& w, const float4 qa, const float4 qb, bool& ha, bool& hb) {
-    ha = near<false>(w, qa, 0, 0, 0, 0.f);
-    hb = near<false>(w, qb, 0, 0, 0, 0.f);
+// Production steps: a member of the 2R set (hit) adds its unit offset to the
+// centrality sum here, in the sweep, and only members inside R go on to the
+// queued phase (by volume the 2R set is about eight times the R set). The
+// centrality sum is a float sum, compared to rounding like the forces (set
+// membership never reads it), so the unit offset is d * rsqrtf(d2) (a few
+// ulp) instead of a square root and three divisions; the floor 1e-12 on d2
+// matches the 1e-6 floor on the distance. Returns whether the member is inside R.
+__device__ __forceinline__ bool ring(Sweep& w, bool hit, const f3 d, float d2) {
+    if (hit) {
+        w.a.csum = add(w.a.csum, mul(d, rsqrtf(fmaxf(d2, 1e-12f))));
+        w.a.n_g += 1;
+    }
+    return hit && d2 <= w.r2;
 }
 
 // Cheap phase over one contiguous candidate range [sc, ec) (wide paths).
@@ -206,7 +214,15 @@ __device__ __forceinline__ void sweep(Sweep& w, uint32_t sc, uint32_t ec, uint32
     for (uint32_t base = sc; base < ec; base += 32) {
         const uint32_t t = base + lane;
         bool hit = false;
-        if (t < ec && t != w.self) hit = near<CHECK_CELL>(w, __ldg(&w.pos[t + w.shift]), cx, cy, cz, inv_cell);
+        if (t < ec && t != w.self) {
+            const float4 q = __ldg(&w.pos[t + w.shift]);
+            f3 d;
+            const float d2 = offset2(w, q, d);
+            hit = d2 <= w.c2;
+            if (CHECK_CELL)
+                hit = hit && pcell(q.x, inv_cell) == cx && pcell(q.y, inv_cell) == cy && pcell(q.z, inv_cell) == cz;
+            if (!SETS) hit = ring(w, hit, d, d2);
+        }
         enqueue<SETS>(w, hit, t, lane);
     }
 }
@@ -253,10 +269,13 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
         // invalid lanes read the bird's own slot (always in range) and discard it
         const float4 qA = ldpos<STG>(&w.pos[(vA ? tA : w.self) + w.shift]);
         const float4 qB = ldpos<STG>(&w.pos[(vB ? tB : w.self) + w.shift]);
-        bool hA, hB;
-        near2(w, qA, qB, hA, hB);
-        hA = hA && vA;
-        hB = hB && vB;
+        f3 dA, dB;
+        const float d2A = offset2(w, qA, dA), d2B = offset2(w, qB, dB);
+        bool hA = vA && d2A <= w.c2, hB = vB && d2B <= w.c2;
+        if (!SETS) {
+            hA = ring(w, hA, dA, d2A);
+            hB = ring(w, hB, dB, d2B);
+        }
         enqueue2<SETS, STG>(w, hA, tA, hB, tB, lane);
     }
 }
