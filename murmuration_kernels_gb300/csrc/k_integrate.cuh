@@ -7,6 +7,65 @@
 
 namespace flk {
 
+// One bird's flight step (model.rs:149-176): the roll follows the bank the
+// lateral steering asks for, then lift, drag, gravity and the control force
+// change the velocity, the speed is clamped and the position advances.
+// a = position, roll; bv = velocity, spin; c = steering, radius; na, nb get
+// the new A and B words. Position, velocity, roll and spin are held to a
+// tolerance (1e-5 relative per bird against the oracle), not bit for bit; the
+// exact words (next decision, neighbour count, radius) come from decide. So
+// the pass uses the cheap forms that tolerance allows: reciprocal square
+// roots for the norms, fast sine/cosine (|beta| <= MAX_BANK) and division, and
+// constant divisors folded into multiplications. The pass is issue-bound, so
+// its instruction count sets its time.
+__device__ __forceinline__ void fly(const float4 a, const float4 bv, const float4 c, float4& na, float4& nb) {
+    constexpr float INV_MASS_G = 1.0f / (MASS * G);
+    constexpr float INV_TAU_ROLL = 1.0f / TAU_ROLL;
+    constexpr float INV_V0 = 1.0f / V0;
+    constexpr float DT_MASS = DT / MASS;
+    f3 vel = xyz(bv);
+    const f3 steering = xyz(c);
+    const float roll = a.w;
+    // forward(vel) and |vel|
+    const float vv = dot(vel, vel);
+    const float ivl = rsqrtf(vv);
+    const float vlen = vv > 0.f ? __fmul_rn(vv, ivl) : 0.f;
+    const f3 fw = vv > 1e-12f ? mul(vel, ivl) : mk(1.f, 0.f, 0.f);
+    // side_of(fw): cross(fw, z) = (fw.y, -fw.x, 0), normalised
+    const float s2 = __fadd_rn(__fmul_rn(fw.x, fw.x), __fmul_rn(fw.y, fw.y));
+    const f3 side = s2 > 1e-8f ? mul(mk(fw.y, -fw.x, 0.f), rsqrtf(s2)) : mk(1.f, 0.f, 0.f);
+    const float speed = fmaxf(vlen, 1e-6f);
+    const float ss = dot(steering, side);
+    const float target = clampf(atanf(__fmul_rn(ss, INV_MASS_G)), -MAX_BANK, MAX_BANK);
+    const float rate = clampf(__fmul_rn(__fsub_rn(target, roll), INV_TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
+    const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
+    float sb, cb;
+    __sincosf(beta, &sb, &cb);
+    // body_up(fw, beta) = cross(side, fw) cos(beta) + side sin(beta), side.z = 0
+    const f3 up0 = mk(__fmul_rn(side.y, fw.z), -__fmul_rn(side.x, fw.z),
+                      __fsub_rn(__fmul_rn(side.x, fw.y), __fmul_rn(fw.x, side.y)));
+    const f3 up = add(mul(up0, cb), mul(side, sb));
+    const float cos_beta = fmaxf(cb, 0.2f);
+    const float sr = __fmul_rn(speed, INV_V0);
+    const float sr2 = __fmul_rn(sr, sr);
+    const float lift = __fdividef(__fmul_rn(sr2, L0), cos_beta);
+    const float drag = __fmul_rn(sr2, D0);
+    const f3 flight = sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mk(0.f, 0.f, __fmul_rn(MASS, G)));
+    const f3 control = sub(steering, mul(side, ss));
+    vel = add(vel, mul(add(control, flight), DT_MASS));
+    const float sp2 = dot(vel, vel);
+    const float isp = rsqrtf(sp2);
+    const float sp = sp2 > 0.f ? __fmul_rn(sp2, isp) : 0.f;
+    if (sp > V_MAX) {
+        vel = mul(vel, __fmul_rn(V_MAX, isp));
+    } else if (sp < V_MIN && sp > 1e-6f) {
+        vel = mul(vel, __fmul_rn(V_MIN, isp));
+    }
+    const f3 pos = add(xyz(a), mul(vel, DT));
+    na = make_float4(pos.x, pos.y, pos.z, beta);
+    nb = make_float4(vel.x, vel.y, vel.z, rate);
+}
+
 // ---------------------------------------------------------------------------
 // pass 6: integrate (model.rs:149-176) + end-of-step bookkeeping
 // ---------------------------------------------------------------------------
@@ -44,45 +103,12 @@ __global__ void __launch_bounds__(256) k_integrate(FlockDesc* __restrict__ fl, i
                 const float4 a = A[st];
                 const float4 bv = B[st];
                 const float4 c = C[st];
-                f3 vel = xyz(bv);
-                const f3 steering = xyz(c);
-                const float roll = a.w;
-
-                // forward(vel), side_of(forward), |vel| and body_up's cos/sin,
-                // each evaluated once with the helpers' exact operations
-                const float vv = dot(vel, vel);
-                const float vlen = __fsqrt_rn(vv);
-                const f3 fw = vv > 1e-12f ? mul(vel, __fdiv_rn(1.0f, vlen)) : mk(1.f, 0.f, 0.f);
-                const f3 side = side_of(fw);
-                const float speed = fmaxf(vlen, 1e-6f);
-                const float ss = dot(steering, side);
-                const float a_lat = __fdiv_rn(ss, MASS);
-                const float target = clampf(atanf(__fdiv_rn(a_lat, G)), -MAX_BANK, MAX_BANK);
-                const float rate = clampf(__fdiv_rn(__fsub_rn(target, roll), TAU_ROLL), -MAX_ROLL_RATE, MAX_ROLL_RATE);
-                const float beta = clampf(__fadd_rn(roll, __fmul_rn(rate, DT)), -MAX_BANK, MAX_BANK);
-
-                const float cb = cosf(beta), sb = sinf(beta);
-                const f3 up = add(mul(cross(side, fw), cb), mul(side, sb));  // body_up(fw, beta)
-                const float cos_beta = fmaxf(cb, 0.2f);
-                const float sr = __fdiv_rn(speed, V0);
-                const float sr2 = __fmul_rn(sr, sr);
-                const float lift = __fdiv_rn(__fmul_rn(sr2, L0), cos_beta);
-                const float drag = __fmul_rn(sr2, D0);
-                const f3 flight =
-                    sub(add(sub(mul(up, lift), mul(fw, drag)), mul(fw, D0)), mul(mul(mk(0.f, 0.f, 1.f), MASS), G));
-                const f3 control = sub(steering, mul(side, ss));
-                vel = add(vel, mul(dvs(add(control, flight), MASS), DT));
-                const float sp = len(vel);
-                if (sp > V_MAX) {
-                    vel = mul(vel, __fdiv_rn(V_MAX, sp));
-                } else if (sp < V_MIN && sp > 1e-6f) {
-                    vel = mul(vel, __fdiv_rn(V_MIN, sp));
-                }
-                const f3 pos = add(xyz(a), mul(vel, DT));
-                A[st] = make_float4(pos.x, pos.y, pos.z, beta);
-                B[st] = make_float4(vel.x, vel.y, vel.z, rate);
+                float4 na, nb;
+                fly(a, bv, c, na, nb);
+                A[st] = na;
+                B[st] = nb;
                 if (FUSE && rem >= 2) {  // this flock steps again: its bird's cell for the next step
-                    b = bucket_slab<true>(make_float4(pos.x, pos.y, pos.z, 0.f), d->bbase, d->buckets, slab,
+                    b = bucket_slab<true>(na, d->bbase, d->buckets, slab,
                                           inv_cell, __fmul_rn(4.0f, inv_cell));
                     key[v] = b;
                     act = true;
