@@ -118,10 +118,12 @@ __device__ __forceinline__ void take(Sweep& w, uint32_t t) {
     }
     w.a.n_all += 1;
     if (SETS) w.a.h_all += set_mix(j);
+    // the separation Gaussian only weights a sum (compared to rounding), so it
+    // takes the fast exponential and a multiplication by 1 / (2 sigma^2)
     float g = 1.0f;
     if (dist > R_H) {
         const float tt = __fsub_rn(dist, R_H);
-        g = expf(__fdiv_rn(-__fmul_rn(tt, tt), TWO_SIGMA2));
+        g = __expf(__fmul_rn(-__fmul_rn(tt, tt), 1.0f / TWO_SIGMA2));
     }
     w.a.sep = sub(w.a.sep, mul(dh, g));
     if (dist > R_H) {
@@ -344,13 +346,13 @@ __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* _
 // Per-warp shared memory: the hit queue and 32 reduced birds awaiting their epilogue.
 template <bool SETS>
 struct WarpSmem {
-    static constexpr int NI = SETS ? 8 : 4;  // integer sums per bird
+    static constexpr int NI = SETS ? 8 : 1;  // integer sums per bird (production steps: in red)
     int4 box[32];          // the next 32 birds' search boxes (group_boxes)
     uint4 aux[32];
     int2 zc[32];           // their first cell along z and cell count along z
     uint32_t queue[96];
-    float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz, 4 unused
-    uint32_t cnt[NI][32];  // n_all, n_star, n_align, n_g (+ the four set hashes)
+    float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz (+ the four counts, production steps)
+    uint32_t cnt[NI][32];  // grid-reporting steps: n_all, n_star, n_align, n_g, the four set hashes
     uint32_t st[32];       // slot of the bird in the reordered buffer
     uint32_t vix[32];      // view index (set summaries)
     float pz[32];          // height (roost pull)
@@ -403,7 +405,13 @@ __device__ __forceinline__ void epilogue(const WarpSmem<SETS>& m, uint32_t slot,
     const f3 coh = mk(m.red[3][slot], m.red[4][slot], m.red[5][slot]);
     const f3 align = mk(m.red[6][slot], m.red[7][slot], m.red[8][slot]);
     const f3 csum = mk(m.red[9][slot], m.red[10][slot], m.red[11][slot]);
-    const uint32_t n_all = m.cnt[0][slot], n_star = m.cnt[1][slot], n_align = m.cnt[2][slot], n_g = m.cnt[3][slot];
+    uint32_t n_all, n_star, n_align, n_g;
+    if (SETS) {
+        n_all = m.cnt[0][slot], n_star = m.cnt[1][slot], n_align = m.cnt[2][slot], n_g = m.cnt[3][slot];
+    } else {
+        n_all = __float2uint_rn(m.red[12][slot]), n_star = __float2uint_rn(m.red[13][slot]);
+        n_align = __float2uint_rn(m.red[14][slot]), n_g = __float2uint_rn(m.red[15][slot]);
+    }
     const f3 v = xyz(Bv[st]);
     const float4 cme = C[st];
     const float nd = D[st].x;
@@ -494,8 +502,11 @@ __device__ __forceinline__ void sweep_bird(Sweep& w, const WarpSmem<SETS>& m, ui
                 // nearest xy point the sphere spans |dz| <= sqrt(reach^2 - dxy^2)
                 // (dxy^2 a lower bound for any bird of the cell). The 1e-4 reach^2
                 // under the root, and the reach's own absolute margin, cover the
-                // rounding; the bird's whole z-range zlo..zhi bounds it.
-                const float hz = __fsqrt_rn(fmaxf(reach2 - dxy2, 0.f) + 1e-4f * reach2);
+                // rounding (and the few ulp of the reciprocal square root, the
+                // argument being at least 1e-4 reach^2 > 0); the bird's whole
+                // z-range zlo..zhi bounds it.
+                const float hz2 = fmaxf(reach2 - dxy2, 0.f) + 1e-4f * reach2;
+                const float hz = hz2 * rsqrtf(hz2);
                 const float inv4 = __fmul_rn(4.0f, inv_cell);
                 z0 = min(3, max(0, max(zlo, pcell(p.z - hz, inv4)) - 4 * cz));
                 z1 = min(3, max(0, min(zhi, pcell(p.z + hz, inv4)) - 4 * cz));
@@ -599,22 +610,21 @@ __device__ __forceinline__ void finish_bird(Sweep& w, WarpSmem<SETS>& m, uint32_
                                             float pz, const Arena& ar, const float* __restrict__ rtab,
                                             uint32_t* __restrict__ sets, uint32_t lane, uint32_t& pairs) {
     {
+        // production steps carry the four counts in the float reduction's spare
+        // slots: per-lane counts are small integers, so their f32 sums are exact
         float fv[16] = {w.a.sep.x,   w.a.sep.y,   w.a.sep.z,   w.a.coh.x,  w.a.coh.y,  w.a.coh.z,
                         w.a.align.x, w.a.align.y, w.a.align.z, w.a.csum.x, w.a.csum.y, w.a.csum.z,
-                        0.f,         0.f,         0.f,         0.f};
+                        SETS ? 0.f : (float)w.a.n_all, SETS ? 0.f : (float)w.a.n_star,
+                        SETS ? 0.f : (float)w.a.n_align, SETS ? 0.f : (float)w.a.n_g};
         const float tf = rs_float<16>(fv, lane);
         if ((lane & 1) == 0) m.red[(lane >> 1) & 15][slot] = tf;
+        if (!SETS && lane == 30) pairs += __float2uint_rn(tf);  // lane 30 holds n_g
     }
     if (SETS) {
         uint32_t iv[8] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g, w.a.h_all, w.a.h_star, w.a.h_align, w.a.h_g};
         const uint32_t ti = rs_uint<8>(iv, lane);
         if ((lane & 3) == 0) m.cnt[(lane >> 2) & 7][slot] = ti;
         if (lane == 12) pairs += ti;  // lane 12 holds n_g
-    } else {
-        uint32_t iv[4] = {w.a.n_all, w.a.n_star, w.a.n_align, w.a.n_g};
-        const uint32_t ti = rs_uint<4>(iv, lane);
-        if ((lane & 7) == 0) m.cnt[(lane >> 3) & 3][slot] = ti;
-        if (lane == 24) pairs += ti;  // lane 24 holds n_g
     }
     if (lane == 0) {
         m.st[slot] = st;
