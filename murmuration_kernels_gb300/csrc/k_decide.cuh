@@ -240,11 +240,20 @@ __device__ __forceinline__ void sweep_packed(Sweep& w, uint32_t s, uint32_t e, u
     const uint32_t nz = __ballot_sync(FULL, e > s);
     const uint32_t R = __popc(nz);
     if (!R) return;
-    // lane q takes the q-th non-empty range
-    const int src = lane < R ? (int)__fns(nz, 0, (int)lane + 1) : 0;
-    const uint32_t rs = __shfl_sync(FULL, s, src);
-    uint32_t rl = __shfl_sync(FULL, e - s, src);
-    if (lane >= R) rl = 0;
+    // lane q takes the q-th non-empty range: each non-empty lane writes its
+    // range at its rank among them into the free part of the hit queue
+    // (w.qn < 32 entries wait, so the 64 words from w.qn fit its 96), and lane
+    // q reads entry q back
+    uint32_t* scratch = w.q + w.qn;
+    if (e > s) {
+        const uint32_t r = __popc(nz & lanemask_lt());
+        scratch[r] = s;
+        scratch[32 + r] = e - s;
+    }
+    __syncwarp();
+    const uint32_t rs = lane < R ? scratch[lane] : 0u;
+    const uint32_t rl = lane < R ? scratch[32 + lane] : 0u;
+    __syncwarp();
     uint32_t inc = rl;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
