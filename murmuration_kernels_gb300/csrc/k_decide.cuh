@@ -523,11 +523,16 @@ __device__ __forceinline__ void sweep_bird(Sweep& w, const WarpSmem<SETS>& m, ui
             b = bbase + (SETS ? (cell_hash(cx, cy, cz) & (buckets - 1u))
                               : lattice_bucket_bits(cx, cy, cz, aux.w));
         }
-        const uint32_t vm = __ballot_sync(FULL, valid);
-        bool keep = false;
-        if (valid) {
-            const uint32_t peers = __match_any_sync(vm, b);
-            keep = (int)lane == __ffs(peers) - 1;
+        // grid-reporting steps drop buckets shared by two cells of the box (the
+        // reference hash collides); production steps have none to drop (see the
+        // slab trim below: the lattice index repeats only every 16 cells or more)
+        bool keep = valid;
+        if (SETS) {
+            const uint32_t vm = __ballot_sync(FULL, valid);
+            if (valid) {
+                const uint32_t peers = __match_any_sync(vm, b);
+                keep = (int)lane == __ffs(peers) - 1;
+            }
         }
         uint32_t s = 0, en = 0;
         if (keep) {
