@@ -3,9 +3,10 @@
 //
 // The warp first builds the bird's 2R neighbourhood: the cells of a
 // conservative box that intersect the (inflated) 2R sphere. With at most 32
-// cells (2R < 4 m, the usual case), each lane takes one cell and duplicate
-// buckets are dropped with __match_any_sync, so every bucket is swept once and
-// needs no per-candidate cell check. Wider boxes walk the cells 32 at a time
+// cells (2R < 4 m, the usual case), each lane takes one cell; every bucket is
+// swept once and needs no per-candidate cell check (grid-reporting steps drop
+// the reference hash's duplicate buckets with __match_any_sync; the production
+// lattice index never repeats within such a box). Wider boxes walk the cells 32 at a time
 // with the reference's exact cell check (cuda/flock.cu:219-221), and a box
 // wider than the flock itself sweeps the flock's whole range.
 //

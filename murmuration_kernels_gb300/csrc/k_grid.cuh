@@ -55,8 +55,8 @@ __global__ void k_pack(float* __restrict__ w, uint32_t n, uint32_t base, Arena s
 // ---------------------------------------------------------------------------
 // Counts one CTA iteration of birds into grid buffer g: a thread's bird v
 // (act) falls in bucket b, z-slab `slab`. Bucket counts use one atomic per
-// distinct bucket of a warp and give each bird its arrival rank (slab in the
-// top two bits). APPEND (grid-reporting steps): the occupied-bucket list gets
+// run of adjacent lanes with one bucket and give each bird its arrival rank
+// (slab in the top two bits). APPEND (grid-reporting steps): the occupied-bucket list gets
 // one atomic per CTA iteration (the first-seen buckets of all eight warps are
 // placed from a shared-memory prefix), so the single list counter is not hit
 // once per warp; production steps list the occupied buckets in k_place
@@ -67,15 +67,26 @@ __device__ __forceinline__ void count_block(bool act, uint32_t v, uint32_t b, ui
                                             uint32_t* __restrict__ arrival, const GridBuf& g,
                                             StepCtl* __restrict__ ctl, uint32_t (&s_first)[2][8], uint32_t it) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // Birds come in cell order, so equal buckets sit in runs of adjacent lanes:
+    // each maximal run of active lanes with one bucket takes one atomic (its
+    // first lane's) for the run's length, and lane k of the run gets rank
+    // old + k. A bucket that recurs after a gap takes another atomic; ranks stay
+    // distinct, and the sort orders every run by bird, so results do not
+    // depend on them.
     const uint32_t m = __ballot_sync(FULL, act);
+    const uint32_t bp = __shfl_up_sync(FULL, b, 1), bn = __shfl_down_sync(FULL, b, 1);
+    const bool head = act && (lane == 0 || !((m >> (lane - 1)) & 1u) || bp != b);
+    const bool tail = act && (lane == 31 || !((m >> (lane + 1)) & 1u) || bn != b);
+    const uint32_t H = __ballot_sync(FULL, head), E = __ballot_sync(FULL, tail);
+    uint32_t le;
+    asm("mov.u32 %0, %%lanemask_le;" : "=r"(le));
+    const uint32_t h = 31u - (uint32_t)__clz(H & le);  // this lane's run head (active lanes)
+    uint32_t old = 0;
+    if (head) old = atomicAdd(&g.counts[b], (uint32_t)__ffs(E >> lane));  // the run ends at lane + len - 1
+    old = __shfl_sync(FULL, old, act ? h : lane);
     bool first = false;
     if (act) {
-        const uint32_t peers = __match_any_sync(m, b);
-        const int leader = __ffs(peers) - 1;
-        uint32_t old = 0;
-        if ((int)lane == leader) old = atomicAdd(&g.counts[b], (uint32_t)__popc(peers));
-        old = __shfl_sync(m, old, leader);
-        const uint32_t rank = old + __popc(peers & lanemask_lt());
+        const uint32_t rank = old + (lane - h);
         if (rank >= (1u << 30)) atomicCAS(&ctl->error, 0u, (uint32_t)DEV_BAD_RANGE);  // 2^30 birds in one cell
         arrival[v] = (rank & 0x3FFFFFFFu) | (slab << 30);
         first = rank == 0;
