@@ -286,7 +286,8 @@ int flk_unpin(void* ptr);
  * pos4[4n] (x, y, z, unused) in device memory into caller-owned device
  * buffers (pos4 and offsets 16-byte aligned), on `stream` (a cudaStream_t,
  * NULL = legacy default stream). It is a blocking call: it synchronises that
- * stream before returning. It calls no allocator: its
+ * stream before returning, so it cannot run under stream capture or inside a
+ * CUDA graph. It calls no allocator: its
  * scratch is one fixed device array inside the library (about 2.5 MiB, held on
  * every GPU that loads the library until exit), sized for at most
  * FLK_NOALLOC_MAX_BIRDS birds; larger n returns FLK_ERR_CAPACITY. Each call
