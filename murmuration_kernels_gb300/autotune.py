@@ -27,7 +27,7 @@ import os
 from typing import Optional
 
 SPACE = {
-    "cell": [3.0, 3.5, 4.0, 5.0],
+    "cell": [3.5, 3.75, 4.0, 4.5],
     "stream_bps": [4, 8, 16],
     "decide_bps": [1, 2, 4, 8],
     "decide_threads": [256, 512, 1024],

@@ -3,7 +3,7 @@
 //
 // The warp first builds the bird's 2R neighbourhood: the cells of a
 // conservative box that intersect the (inflated) 2R sphere. With at most 32
-// cells (2R < 4 m, the usual case), each lane takes one cell; every bucket is
+// cells (2R below about one cell edge, the usual case), each lane takes one cell; every bucket is
 // swept once and needs no per-candidate cell check (grid-reporting steps drop
 // the reference hash's duplicate buckets with __match_any_sync; the production
 // lattice index never repeats within such a box). Wider boxes walk the cells 32 at a time

@@ -84,9 +84,9 @@ def test_cell_axis_is_searched_first_and_kept_only_when_faster(tmp_path, monkeyp
     at = _autotune()
     monkeypatch.setattr(at, "CACHE", str(tmp_path / "autotune.json"))
     assert list(at.SPACE)[0] == "cell" and at.DEFAULT["cell"] == 4.0
-    # a 5 m cell is 3 % faster for this mix; every other knob is neutral
-    cost = lambda s: 0.97 if s["cell"] == 5.0 else 1.0
+    # a 4.5 m cell is 3 % faster for this mix; every other knob is neutral
+    cost = lambda s: 0.97 if s["cell"] == 4.5 else 1.0
     b = FakeBatch(cost)
     r = at.tune(b, steps=10, use_cache=False)
-    assert r["shape"]["cell"] == 5.0 and b.shape["cell"] == 5.0
+    assert r["shape"]["cell"] == 4.5 and b.shape["cell"] == 4.5
     assert {k: v for k, v in r["shape"].items() if k != "cell"} == {k: v for k, v in at.DEFAULT.items() if k != "cell"}

@@ -284,12 +284,12 @@ def test_dense_production_cell_and_long_runs(native, oracle):
     assert_step_parity(native, oracle, np.concatenate([w, oracle.scatter(3000, 17)]))
 
 
-@pytest.mark.parametrize("cell", [2.5, 3.0, 4.0, 5.0])
+@pytest.mark.parametrize("cell", [2.5, 3.0, 3.5, 3.75, 4.0, 4.5, 5.0])
 def test_production_cell_edges_decide_the_same(native, oracle, cell):
     # the production cell edge changes which candidates decide tests, never the
-    # neighbours it finds: every edge the autotuner may pick (3, 3.5, 4, 5 m
-    # among them) and one whose boxes mostly take the cell walk (2.5 m), from
-    # the same state
+    # neighbours it finds: every edge the autotuner may pick (3.5, 3.75, 4 (the
+    # default, the reference's) and 4.5 m), wider and narrower ones, and one
+    # whose boxes mostly take the cell walk (2.5 m), from the same state
     w = native.generate(100_000, 1)
     t_cpu, c, _, _ = oracle.step(w, 0.0)
     f = native.Flock(w)
