@@ -1,6 +1,6 @@
 """The reference's own CUDA kernels, driven through the CUDA driver API.
 
-TEST AND BASELINE INFRASTRUCTURE ONLY: used by tests/golden/make_reference_fixtures.py
+Test and reference-timing infrastructure only: used by tests/golden/make_reference_fixtures.py
 (golden fixtures) and by bench.py's reference-kernel baseline. The product
 package never imports it.
 
