@@ -24,13 +24,13 @@
 // full warps instead of running it for a few lanes. The cheap phase sweeps the
 // bucket ranges as one packed sequence, two 32-candidate chunks per iteration
 // (two loads in flight per lane).
-// The per-bird box arithmetic runs one bird per lane for a warp's next 32
-// birds (group_boxes), not warp-uniformly.
+// The per-bird box arithmetic runs one bird per lane for a warp's next
+// DECIDE_BATCH birds (group_boxes), not warp-uniformly.
 //
 // Per-lane partial sums are reduced with a transposed (reduce-scatter)
-// shuffle pattern straight into shared memory; once 32 birds are reduced, all
-// lanes finish their decisions at once, one bird per lane, in the oracle's
-// order of operations.
+// shuffle pattern straight into shared memory; once DECIDE_BATCH birds are
+// reduced, the lanes finish their decisions at once, one bird per lane, in the
+// oracle's order of operations.
 #pragma once
 
 #include "device_common.cuh"
@@ -353,23 +353,30 @@ __device__ __forceinline__ float radius_step(float r, uint32_t n, const float* _
     return clampf(__fmul_rn(r, factor), R_H, R_MAX);
 }
 
-// Per-warp shared memory: the hit queue and 32 reduced birds awaiting their epilogue.
+// Birds a warp batches: their search boxes are computed together
+// (group_boxes, one bird per lane) and their decisions finished together (the
+// epilogue, one bird per lane). Shared memory and the L1 cache share each SM's
+// storage, so a smaller batch leaves decide's candidate reads more L1.
+constexpr uint32_t DECIDE_BATCH = 8;
+
+// Per-warp shared memory: the hit queue and the batch's reduced birds awaiting
+// their epilogue.
 template <bool SETS>
 struct WarpSmem {
     static constexpr int NI = SETS ? 8 : 1;  // integer sums per bird (production steps: in red)
-    int4 box[32];          // the next 32 birds' search boxes (group_boxes)
-    uint4 aux[32];
-    int2 zc[32];           // their first cell along z and cell count along z
+    int4 box[DECIDE_BATCH];          // the batch's search boxes (group_boxes)
+    uint4 aux[DECIDE_BATCH];
+    int2 zc[DECIDE_BATCH];           // their first cell along z and cell count along z
     uint32_t queue[96];
-    float red[16][32];     // sep xyz, coh xyz, align xyz, csum xyz (+ the four counts, production steps)
-    uint32_t cnt[NI][32];  // grid-reporting steps: n_all, n_star, n_align, n_g, the four set hashes
-    uint32_t st[32];       // slot of the bird in the reordered buffer
-    uint32_t vix[32];      // view index (set summaries)
-    float pz[32];          // height (roost pull)
+    float red[16][DECIDE_BATCH];     // sep xyz, coh xyz, align xyz, csum xyz (+ the four counts, production steps)
+    uint32_t cnt[NI][DECIDE_BATCH];  // grid-reporting steps: n_all, n_star, n_align, n_g, the four set hashes
+    uint32_t st[DECIDE_BATCH];       // slot of the bird in the reordered buffer
+    uint32_t vix[DECIDE_BATCH];      // view index (set summaries)
+    float pz[DECIDE_BATCH];          // height (roost pull)
 };
 
-// Search boxes of a warp's next 32 deciding birds (records e, e + nw, ...,
-// e + 31 nw), one bird per lane, so the box arithmetic runs once per bird
+// Search boxes of a warp's next DECIDE_BATCH deciding birds (records e,
+// e + nw, ...), one bird per lane, so the box arithmetic runs once per bird
 // rather than once per lane of a warp-uniform setup. Cells of edge
 // 1 / inv_cell (the reference's 4 m cells in SETS steps). box: first cell x,
 // y; the z-slab range floor((z -/+ reach) * 4 inv_cell) (slabs of a quarter
@@ -381,7 +388,7 @@ template <bool SETS>
 __device__ __forceinline__ void group_boxes(WarpSmem<SETS>& m, const DueRec* __restrict__ due, uint32_t e,
                                             uint32_t nw, uint32_t ndue, uint32_t lane, float inv_cell) {
     const uint32_t ej = e + lane * nw;
-    if (ej < ndue) {
+    if (lane < DECIDE_BATCH && ej < ndue) {
         const float4 pr = due[ej].pr;
         const uint32_t buckets = due[ej].fl.z;
         const SearchBox sb = search_box(mk(pr.x, pr.y, pr.z), pr.w, inv_cell);
@@ -619,7 +626,7 @@ __device__ __forceinline__ void sweep_bird(Sweep& w, const WarpSmem<SETS>& m, ui
 
 // Reduces the warp's sums for the current bird (slot `slot` of the batch, its
 // slot st in the state, view index k, height pz) and runs the batch's
-// epilogue once 32 birds wait.
+// epilogue once DECIDE_BATCH birds wait.
 template <bool SETS>
 __device__ __forceinline__ void finish_bird(Sweep& w, WarpSmem<SETS>& m, uint32_t& slot, uint32_t st, uint32_t k,
                                             float pz, const Arena& ar, const float* __restrict__ rtab,
@@ -646,9 +653,9 @@ __device__ __forceinline__ void finish_bird(Sweep& w, WarpSmem<SETS>& m, uint32_
         m.vix[slot] = k;
         m.pz[slot] = pz;
     }
-    if (++slot == 32) {
+    if (++slot == DECIDE_BATCH) {
         __syncwarp();
-        epilogue<SETS>(m, lane, ar, rtab, sets);
+        if (lane < DECIDE_BATCH) epilogue<SETS>(m, lane, ar, rtab, sets);
         __syncwarp();
         slot = 0;
     }
