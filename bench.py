@@ -352,8 +352,8 @@ def pass_bandwidths(r, n):
 # PROFILED_AT; 4 warp instructions per clock per SM peak. Both this figure and
 # the step traffic in profiles/traffic_step_1m.txt are re-taken whenever the
 # kernels change.
-DECIDE_INST_1M = 105.0e6
-PROFILED_AT = "765f4a8"
+DECIDE_INST_1M = 109.0e6
+PROFILED_AT = "2758cb7"
 GB300_SMS = 152
 
 
