@@ -6,7 +6,8 @@
 // every bird integrates. The passes here:
 //
 //   k_hash_count  cell key per bird + bucket histogram with warp-aggregated
-//                 atomics (__match_any_sync); records each bird's arrival rank
+//                 atomics (one per run of adjacent lanes with one bucket);
+//                 records each bird's arrival rank
 //                 and, in grid-reporting steps, appends first-seen buckets to
 //                 an occupied-bucket list (one atomic per CTA iteration).
 //                 Production steps bucket cells by a lattice index,
@@ -24,8 +25,8 @@
 //                 flock's two state buffers in that order; it also writes each
 //                 bird's unit heading and stages the deciding-bird records.
 //   k_decide      one warp per deciding bird, one 1024-thread CTA per SM: the
-//                 2R neighbourhood's buckets (deduplicated with
-//                 __match_any_sync) are swept as one packed sequence of
+//                 2R neighbourhood's buckets (deduplicated with __match_any_sync
+//                 in grid-reporting steps) are swept as one packed sequence of
 //                 candidates, hits are queued and processed on full warps,
 //                 and a reduce-scatter of shuffles sums them.
 //   k_integrate   banked flight, streaming float4 over the reordered buffer;
